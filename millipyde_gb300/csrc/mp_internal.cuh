@@ -1,0 +1,218 @@
+// mp_internal.cuh -- shared definitions of the CUDA side of millipyde_gb300.
+//
+// Kernel descriptors (MPJob), the pointwise-op interpreter used as prologue /
+// epilogue of every kernel kind, and the inline-PTX wrappers for mbarrier and
+// TMA (cp.async.bulk.tensor) used by the gaussian kernel.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/millipyde_gb300.h"
+
+// ---------------------------------------------------------------------------
+// Limits
+// ---------------------------------------------------------------------------
+#define MP_MAX_PW 8                       // pointwise ops in one prologue/epilogue
+#define MP_MAX_TAPS (2 * MP_MAX_RADIUS + 1)
+#define MP_FIX_FRAC 40                    // fractional bits of rotate coordinates
+#define MP_SPIN_FAST 2048                 // try_wait polls before backing off
+#define MP_SPIN_LIMIT (1u << 21)          // bounded wait: ~2 s with 1 us backoff
+
+// Segment kernel kinds.
+enum MPKind { MPK_POINT = 0, MPK_GAUSS = 1, MPK_ROTATE = 2, MPK_TRANSPOSE = 3 };
+
+// Device-side error word values (written by kernels, read by the host).
+enum { MP_KERR_NONE = 0, MP_KERR_TIMEOUT = 1 };
+
+struct PwOp {
+    int op;        // MP_OP_RGB2GREY / BRIGHTNESS / ADJUST_GAMMA / COLORIZE
+    float p0, p1, p2;
+};
+
+struct PwList {
+    int n;
+    PwOp op[MP_MAX_PW];
+};
+
+// One image's work for one segment kernel.  The tensor map member makes the
+// struct 128-byte aligned, so every entry of a job table in global memory
+// holds a legal TMA descriptor address.
+struct MPJob {
+    CUtensorMap tmap;          // GAUSS: 2-D map over the source, box {64, th+2r}
+    const float *src;
+    float *dst;
+    long long cosq, sinq;      // ROTATE: cos/sin * 2^(MP_FIX_FRAC-1), rounded
+    int h, w;                  // source height/width (pixels)
+    int ho, wo;                // output height/width
+    int src_pitch, dst_pitch;  // row pitches in floats
+    int cin, cmid, cout;       // channels: source, after prologue, after epilogue
+    int flip;                  // output map: mirror x (fliplr)
+    int radius;                // GAUSS radius
+    int tw, th;                // tile size (pixels)
+    int tiles_x;               // tiles across this image
+    int tile0;                 // first global tile index of this image
+    int ntiles;                // tiles of this image
+    int use_tma;               // GAUSS: source rows 16-byte aligned -> TMA path
+    PwList pro, epi;
+    float wts[MP_MAX_TAPS];    // GAUSS: normalised taps w[0..2r]
+};
+
+// ---------------------------------------------------------------------------
+// Pointwise ops.  Semantics follow the reference's per-pixel formulas
+// (src/millipyde_image.cpp:64 grey, :392-394 brightness, :447-452 gamma,
+// :494-524 colorize), in float32 on values in [0,1]; alpha (channel 3 of a
+// 4-channel pixel) is left untouched as in the reference's RGBA kernels.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float mp_clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+
+// Applies L to v[0..c-1] and returns the new channel count.
+__device__ __forceinline__ int mp_pw_apply(const PwList &L, float v[4], int c)
+{
+    for (int i = 0; i < L.n; ++i) {
+        const PwOp o = L.op[i];
+        const int cc = (c == 4) ? 3 : c;     // colour channels
+        switch (o.op) {
+        case MP_OP_RGB2GREY:
+            if (c >= 3) {
+                v[0] = fminf(1.0f, 0.2125f * v[0] + 0.7154f * v[1] + 0.0721f * v[2]);
+                c = 1;
+            }
+            break;
+        case MP_OP_BRIGHTNESS:
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (k < cc) v[k] = mp_clamp01(v[k] + o.p0);
+            break;
+        case MP_OP_ADJUST_GAMMA:
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (k < cc) v[k] = mp_clamp01(o.p1 * powf(v[k], o.p0));
+            break;
+        case MP_OP_COLORIZE:
+            if (c >= 3) {
+                v[0] = fminf(1.0f, v[0] * o.p0);
+                v[1] = fminf(1.0f, v[1] * o.p1);
+                v[2] = fminf(1.0f, v[2] * o.p2);
+            }
+            break;
+        default:
+            break;
+        }
+    }
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier / TMA wrappers (PTX ISA 8.x, sm_90+; compiled for sm_103a).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t mp_smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mp_mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mp_smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mp_fence_barrier_init()
+{
+    // Make the initialised barrier visible to the async (TMA) proxy.
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mp_mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     mp_smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mp_mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(mp_smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false if the phase did not complete within
+// MP_SPIN_LIMIT polls (about two seconds), so a lost transfer turns into an
+// error status instead of a hung GPU.
+__device__ __forceinline__ bool mp_mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < MP_SPIN_LIMIT; ++i) {
+        if (mp_mbar_try_wait(bar, parity)) return true;
+        if (i >= MP_SPIN_FAST) __nanosleep(1000);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mp_tensormap_acquire(const CUtensorMap *map)
+{
+    // The map may live in global memory (batch job table); order the generic
+    // writes that produced it before the TMA unit reads it.
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
+
+__device__ __forceinline__ void mp_tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar,
+                                               int x, int y)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%3, %4}], [%2];" ::"r"(mp_smem_addr(dst)),
+        "l"(map), "r"(mp_smem_addr(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// Host-side helpers shared by the .cu files of the library.
+// ---------------------------------------------------------------------------
+#ifdef __cplusplus
+void mp_set_cuda_error(cudaError_t e);
+// Converts a CUDA error into an MPStatus, remembering its text.
+MPStatus mp_cuda_status(cudaError_t e);
+#define MP_CUDA_TRY(expr)                                    \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) return mp_cuda_status(_e);    \
+    } while (0)
+
+// Per-device error word the kernels write (MP_KERR_*).
+int *mp_device_error_word(int device);
+// Reads and clears the error word; MP_ERROR_KERNEL_TIMEOUT if set.
+MPStatus mp_check_device_error(cudaStream_t stream);
+
+// Tensor-map encoder from the driver (looked up at run time).
+typedef CUresult (*mp_encode_tiled_fn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                       const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                       const cuuint32_t *, CUtensorMapInterleave,
+                                       CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                       CUtensorMapFloatOOBfill);
+mp_encode_tiled_fn mp_get_encode_tiled();
+
+// Stream-ordered allocation from the device's memory pool.
+MPStatus mp_malloc_async(void **p, size_t bytes, cudaStream_t s);
+void mp_free_async(void *p, cudaStream_t s);
+
+// Kernel launchers (mp_kernels.cu).  `jobs` is a device table of njobs jobs
+// sorted by tile0; `total_tiles` the sum of their ntiles.
+MPStatus mp_launch_kind(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
+                        size_t smem_bytes, cudaStream_t s);
+// Single-job launch with the job passed by value (no device table).
+MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem_bytes, cudaStream_t s);
+// In-place channel-agnostic pointwise list over n contiguous floats.
+MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s);
+// Dynamic shared memory a GAUSS launch needs for the given geometry.
+size_t mp_gauss_smem_bytes(int tw, int th, int radius, int cin, int cmid, int has_pro);
+#endif

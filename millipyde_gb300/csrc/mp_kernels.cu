@@ -1,0 +1,543 @@
+// mp_kernels.cu -- sm_103a kernels of the image hot path.
+//
+// Four segment kernels, each able to run a pointwise prologue (applied to
+// every source value it reads) and a pointwise epilogue (applied to every
+// value it writes), plus an optional fliplr output map:
+//   POINT      pointwise only                       (rgb2grey, brightness, gamma, colorize, fliplr)
+//   GAUSS      separable zero-padded gaussian       (src/millipyde_image.cpp:146-244, radius ceil(3 sigma))
+//   ROTATE     bilinear rotation about (W/2, H/2)   (src/millipyde_image.cpp:114-139 geometry)
+//   TRANSPOSE  out[x][y] = in[y][x]                 (src/millipyde_image.cpp:73-96)
+// Every kernel reads its work from an MPJob (one per image).  A launch covers
+// a ragged batch: blockIdx.x is a global tile index, mapped to its image by a
+// binary search over the jobs' tile offsets.
+#include "mp_internal.cuh"
+
+#define MP_THREADS 256
+
+// ---------------------------------------------------------------------------
+// Job lookup
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int mp_find_job(const MPJob *__restrict__ jobs, int njobs, int tile)
+{
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].tile0 <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// GAUSS shared-memory layout (host and device agree on it).
+//   [0,16)        mbarrier
+//   [16, 16+4*T)  taps (T = MP_MAX_TAPS, rounded to 16 floats)
+//   A (128-B aligned): TMA tile S, later vT (prologue) or obuf (no prologue)
+//   B (128-B aligned): vT (no prologue) or G then obuf (prologue)
+// All sizes in floats unless noted.
+// ---------------------------------------------------------------------------
+struct GaussGeom {
+    int BH, nbx_max, JW, GWp, RBp, OBW;
+    int offA, offB;      // byte offsets from the 128-B aligned base
+    int total;           // bytes
+};
+
+__host__ __device__ __forceinline__ int mp_round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+__host__ __device__ __forceinline__ GaussGeom mp_gauss_geom(int tw, int th, int r, int cin,
+                                                            int cmid, int has_pro)
+{
+    GaussGeom g;
+    g.BH = th + 2 * r;
+    g.nbx_max = (3 + (tw + 2 * r) * cin + 63) / 64;
+    g.JW = (tw + 2 * r) * cmid;
+    g.GWp = mp_round_up(g.JW, 4);
+    g.RBp = th + 4;
+    g.OBW = tw * cmid + 1;
+    const int S = g.nbx_max * 64 * g.BH;
+    const int vT = g.JW * g.RBp;
+    const int G = has_pro ? g.BH * g.GWp : 0;
+    const int ob = th * g.OBW;
+    int A, B;
+    if (has_pro) {
+        A = S > vT ? S : vT;
+        B = G > ob ? G : ob;
+    } else {
+        A = S > ob ? S : ob;
+        B = vT;
+    }
+    const int head = mp_round_up(16 + 4 * mp_round_up(MP_MAX_TAPS, 16), 128);
+    g.offA = head;
+    g.offB = g.offA + mp_round_up(A * 4, 128);
+    g.total = g.offB + mp_round_up(B * 4, 128);
+    return g;
+}
+
+size_t mp_gauss_smem_bytes(int tw, int th, int radius, int cin, int cmid, int has_pro)
+{
+    return (size_t)mp_gauss_geom(tw, th, radius, cin, cmid, has_pro).total + 128;  // +128: alignment slack
+}
+
+// 1-D correlation along the row index of a [rows][stride] float array,
+// producing 8 consecutive outputs for 4 consecutive columns:
+//   acc[o] += sum_{m<ntaps} w[m] * base[(o+m)*stride .. +3]
+// Inputs are kept in an 8-entry register ring indexed by row & 7, so each
+// loaded float4 feeds 8 outputs (8 FMAs per float loaded).
+__device__ __forceinline__ void mp_conv8(const float *base, int stride, int ntaps,
+                                         const float *w, float4 acc[8])
+{
+    float4 X[8];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) X[k] = *reinterpret_cast<const float4 *>(base + k * stride);
+    for (int m0 = 0; m0 < ntaps; m0 += 8) {
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const int m = m0 + s;
+            if (m >= ntaps) break;
+            X[(s + 7) & 7] = *reinterpret_cast<const float4 *>(base + (m + 7) * stride);
+            const float wm = w[m];
+#pragma unroll
+            for (int o = 0; o < 8; ++o) {
+                const float4 x = X[(s + o) & 7];
+                acc[o].x = fmaf(wm, x.x, acc[o].x);
+                acc[o].y = fmaf(wm, x.y, acc[o].y);
+                acc[o].z = fmaf(wm, x.z, acc[o].z);
+                acc[o].w = fmaf(wm, x.w, acc[o].w);
+            }
+        }
+    }
+}
+
+// One output tile (tw x th pixels) of a separable gaussian.
+//   1. TMA loads the halo'd source tile (th+2r rows, (tw+2r)*cin floats plus
+//      up to 3 floats of 16-byte alignment slack) as nbx boxes of 64 floats;
+//      rows/columns outside the image arrive as zeros (the zero padding).
+//   2. Optional prologue: pointwise ops into G (zeros kept outside the image).
+//   3. Vertical pass -> vT, stored transposed ([column][row]).
+//   4. Horizontal pass over vT rows -> obuf ([row][x*cmid+c]).
+//   5. Copy-out with epilogue and the fliplr map.
+__device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned char *smem_raw,
+                                              bool map_in_global, int *err)
+{
+    const int r = J.radius, tw = J.tw, th = J.th;
+    const int cin = J.cin, cmid = J.cmid;
+    const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
+    const int x0 = tx * tw, y0 = ty * th;
+    const int has_pro = J.pro.n > 0;
+    const GaussGeom g = mp_gauss_geom(tw, th, r, cin, cmid, has_pro);
+
+    unsigned char *base =
+        smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(base);
+    float *wsm = reinterpret_cast<float *>(base + 16);
+    float *A = reinterpret_cast<float *>(base + g.offA);
+    float *B = reinterpret_cast<float *>(base + g.offB);
+    float *S = A;
+
+    const int gx = (x0 - r) * cin;
+    const int xa = gx & ~3;
+    const int delta = gx - xa;
+    const int nbx = (delta + (tw + 2 * r) * cin + 63) / 64;
+    const int ntaps = 2 * r + 1;
+
+    for (int i = threadIdx.x; i < ntaps; i += blockDim.x) wsm[i] = J.wts[i];
+
+    if (J.use_tma) {
+        if (threadIdx.x == 0) {
+            mp_mbar_init(bar, 1);
+            mp_fence_barrier_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (map_in_global) mp_tensormap_acquire(&J.tmap);
+            mp_mbar_arrive_expect_tx(bar, (uint32_t)(nbx * 64 * g.BH * 4));
+            for (int b = 0; b < nbx; ++b)
+                mp_tma_load_2d(S + b * 64 * g.BH, &J.tmap, bar, xa + 64 * b, y0 - r);
+        }
+        const bool ok = mp_mbar_wait_bounded(bar, 0);
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) atomicExch(err, MP_KERR_TIMEOUT);
+            mp_mbar_wait_bounded(bar, 0);   // let in-flight copies land before exiting
+            return;
+        }
+    } else {
+        // Plain-load fallback for sources whose rows are not 16-byte aligned:
+        // same box-major layout, zeros outside the image.
+        const int rowlen = J.w * cin;
+        const int n = nbx * 64 * g.BH;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int b = i / (64 * g.BH);
+            const int rem = i - b * 64 * g.BH;
+            const int row = rem >> 6, col = rem & 63;
+            const int gyy = y0 - r + row;
+            const int gxx = xa + 64 * b + col;
+            float v = 0.0f;
+            if (gyy >= 0 && gyy < J.h && gxx >= 0 && gxx < rowlen)
+                v = __ldg(J.src + (size_t)gyy * J.src_pitch + gxx);
+            S[i] = v;
+        }
+        __syncthreads();
+    }
+
+    // ---- 2. prologue into G
+    const float *vsrc;
+    int vstride, vdelta, nq;
+    float *vT;
+    float *obuf;
+    if (has_pro) {
+        float *G = B;
+        const int npx = tw + 2 * r;
+        for (int i = threadIdx.x; i < g.BH * npx; i += blockDim.x) {
+            const int row = i / npx, xi = i - row * npx;
+            const int gyy = y0 - r + row, gxx = x0 - r + xi;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            if (gyy >= 0 && gyy < J.h && gxx >= 0 && gxx < J.w) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    if (c < cin) {
+                        const int col = delta + xi * cin + c;
+                        v[c] = S[(col >> 6) * 64 * g.BH + row * 64 + (col & 63)];
+                    }
+                }
+                mp_pw_apply(J.pro, v, cin);
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (c < cmid) G[row * g.GWp + xi * cmid + c] = v[c];
+        }
+        __syncthreads();
+        vsrc = G;
+        vstride = g.GWp;
+        vdelta = 0;
+        nq = g.GWp / 4;
+        vT = A;
+        obuf = B;
+    } else {
+        vsrc = S;
+        vstride = 64;
+        vdelta = delta;
+        nq = (delta + g.JW + 3) / 4;
+        vT = B;
+        obuf = A;
+    }
+
+    // ---- 3. vertical pass: item (q, grp) = 4 columns x 8 output rows
+    const int ngrp = th / 8;
+    for (int it = threadIdx.x; it < nq * ngrp; it += blockDim.x) {
+        const int q = it % nq, grp = it / nq;
+        const float *colbase;
+        if (has_pro) colbase = vsrc + 4 * q;
+        else colbase = vsrc + (q >> 4) * 64 * g.BH + ((q & 15) << 2);
+        float4 acc[8];
+#pragma unroll
+        for (int o = 0; o < 8; ++o) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        mp_conv8(colbase + 8 * grp * vstride, vstride, ntaps, wsm, acc);
+        const int j0 = 4 * q - vdelta;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int j = j0 + k;
+            if (j >= 0 && j < g.JW) {
+                float *dst = vT + j * g.RBp + 8 * grp;
+                float c0[8];
+#pragma unroll
+                for (int o = 0; o < 8; ++o)
+                    c0[o] = (k == 0) ? acc[o].x : (k == 1) ? acc[o].y : (k == 2) ? acc[o].z : acc[o].w;
+                reinterpret_cast<float4 *>(dst)[0] = make_float4(c0[0], c0[1], c0[2], c0[3]);
+                reinterpret_cast<float4 *>(dst)[1] = make_float4(c0[4], c0[5], c0[6], c0[7]);
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- 4. horizontal pass: item (a, c, b) = 4 rows x 8 consecutive x, channel c
+    const int na = th / 4, nb = tw / 8;
+    for (int it = threadIdx.x; it < na * cmid * nb; it += blockDim.x) {
+        const int a = it % na;
+        const int rest = it / na;
+        const int c = rest % cmid, b = rest / cmid;
+        float4 acc[8];
+#pragma unroll
+        for (int o = 0; o < 8; ++o) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        mp_conv8(vT + ((8 * b) * cmid + c) * g.RBp + 4 * a, cmid * g.RBp, ntaps, wsm, acc);
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            float *dst = obuf + (4 * a) * g.OBW + (8 * b + o) * cmid + c;
+            dst[0] = acc[o].x;
+            dst[g.OBW] = acc[o].y;
+            dst[2 * g.OBW] = acc[o].z;
+            dst[3 * g.OBW] = acc[o].w;
+        }
+    }
+    __syncthreads();
+
+    // ---- 5. copy-out with epilogue and output map
+    for (int i = threadIdx.x; i < th * tw; i += blockDim.x) {
+        const int tt = i / tw, xx = i - tt * tw;
+        const int gyy = y0 + tt, gxx = x0 + xx;
+        if (gyy >= J.h || gxx >= J.w) continue;
+        float v[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = (c < cmid) ? obuf[tt * g.OBW + xx * cmid + c] : 0.f;
+        const int co = mp_pw_apply(J.epi, v, cmid);
+        const int xo = J.flip ? (J.wo - 1 - gxx) : gxx;
+        float *dst = J.dst + (size_t)gyy * J.dst_pitch + (size_t)xo * co;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (c < co) dst[c] = v[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ROTATE: 32x32 output tile, 256 threads, 4 rows per thread.  Source
+// coordinates in 64-bit fixed point (MP_FIX_FRAC fractional bits), so the
+// bilinear fractions keep ~24 correct bits even for 8192-wide images.
+//   s = R(theta) (p - c) + c,  c = (W/2, H/2),  p = output pixel
+// Neighbours outside the source contribute 0 (zero fill); the prologue is
+// applied to each in-range neighbour before interpolation.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mp_load_px(const MPJob &J, int ix, int iy, float v[4])
+{
+    v[0] = v[1] = v[2] = v[3] = 0.f;
+    if (ix < 0 || iy < 0 || ix >= J.w || iy >= J.h) return;
+    const float *p = J.src + (size_t)iy * J.src_pitch + (size_t)ix * J.cin;
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        if (c < J.cin) v[c] = __ldg(p + c);
+    if (J.pro.n) mp_pw_apply(J.pro, v, J.cin);
+}
+
+__device__ __forceinline__ void mp_rotate_tile(const MPJob &J, int t)
+{
+    const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
+    const int x = tx * 32 + (threadIdx.x & 31);
+    if (x >= J.wo) return;
+    const long long W = J.w, H = J.h;
+    const long long X2 = 2LL * x - W;
+    const long long cx = W << (MP_FIX_FRAC - 1), cy = H << (MP_FIX_FRAC - 1);
+    const int cmid = J.cmid;
+#pragma unroll 1
+    for (int i = 0; i < 4; ++i) {
+        const int y = ty * 32 + (threadIdx.x >> 5) + 8 * i;
+        if (y >= J.ho) break;
+        const long long Y2 = 2LL * y - H;
+        const long long sx = J.cosq * X2 - J.sinq * Y2 + cx;
+        const long long sy = J.sinq * X2 + J.cosq * Y2 + cy;
+        const int ix = (int)(sx >> MP_FIX_FRAC);
+        const int iy = (int)(sy >> MP_FIX_FRAC);
+        const float fx = (float)((int)((sx >> (MP_FIX_FRAC - 24)) & 0xFFFFFF)) * 5.9604644775390625e-8f;
+        const float fy = (float)((int)((sy >> (MP_FIX_FRAC - 24)) & 0xFFFFFF)) * 5.9604644775390625e-8f;
+        float a[4], b[4], c[4], d[4];
+        mp_load_px(J, ix, iy, a);
+        mp_load_px(J, ix + 1, iy, b);
+        mp_load_px(J, ix, iy + 1, c);
+        mp_load_px(J, ix + 1, iy + 1, d);
+        float v[4];
+        const float gx = 1.0f - fx, gy = 1.0f - fy;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            v[k] = gy * (gx * a[k] + fx * b[k]) + fy * (gx * c[k] + fx * d[k]);
+        const int co = mp_pw_apply(J.epi, v, cmid);
+        const int xo = J.flip ? (J.wo - 1 - x) : x;
+        float *dst = J.dst + (size_t)y * J.dst_pitch + (size_t)xo * co;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (k < co) dst[k] = v[k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// TRANSPOSE: 32x32 source tile through shared memory (+1 float row padding).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mp_transpose_tile(const MPJob &J, int t, float *tile)
+{
+    const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
+    const int x0 = tx * 32, y0 = ty * 32;           // source tile origin
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    const int cmid = J.cmid;
+    const int ld = 32 * 4 + 1;
+    for (int i = 0; i < 4; ++i) {
+        const int y = y0 + ly + 8 * i, x = x0 + lx;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (x < J.w && y < J.h) {
+            const float *p = J.src + (size_t)y * J.src_pitch + (size_t)x * J.cin;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (c < J.cin) v[c] = __ldg(p + c);
+            if (J.pro.n) mp_pw_apply(J.pro, v, J.cin);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (c < cmid) tile[(ly + 8 * i) * ld + lx * cmid + c] = v[c];
+    }
+    __syncthreads();
+    for (int i = 0; i < 4; ++i) {
+        // output pixel (xo, yo) = source (yo, xo): output row = source column
+        const int yo = x0 + ly + 8 * i, xo = y0 + lx;
+        if (yo >= J.ho || xo >= J.wo) continue;
+        float v[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = (c < cmid) ? tile[lx * ld + (ly + 8 * i) * cmid + c] : 0.f;
+        const int co = mp_pw_apply(J.epi, v, cmid);
+        const int xf = J.flip ? (J.wo - 1 - xo) : xo;
+        float *dst = J.dst + (size_t)yo * J.dst_pitch + (size_t)xf * co;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (c < co) dst[c] = v[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// POINT: 256 pixels x 4 rows per tile; prologue then epilogue, fliplr map.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mp_point_tile(const MPJob &J, int t)
+{
+    const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
+    const int x = tx * 256 + threadIdx.x;
+    if (x >= J.w) return;
+    for (int i = 0; i < 4; ++i) {
+        const int y = ty * 4 + i;
+        if (y >= J.h) break;
+        const float *p = J.src + (size_t)y * J.src_pitch + (size_t)x * J.cin;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (c < J.cin) v[c] = __ldg(p + c);
+        int cc = mp_pw_apply(J.pro, v, J.cin);
+        cc = mp_pw_apply(J.epi, v, cc);
+        const int xo = J.flip ? (J.wo - 1 - x) : x;
+        float *dst = J.dst + (size_t)y * J.dst_pitch + (size_t)xo * cc;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (c < cc) dst[c] = v[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Kernel entry points
+// ---------------------------------------------------------------------------
+template <int KIND>
+__device__ __forceinline__ void mp_run_tile(const MPJob &J, int lt, bool map_in_global, int *err)
+{
+    extern __shared__ unsigned char mp_dyn_smem[];
+    if (KIND == MPK_GAUSS) {
+        mp_gauss_tile(J, lt, mp_dyn_smem, map_in_global, err);
+    } else if (KIND == MPK_ROTATE) {
+        mp_rotate_tile(J, lt);
+    } else if (KIND == MPK_TRANSPOSE) {
+        __shared__ float tile[32 * (32 * 4 + 1)];
+        mp_transpose_tile(J, lt, tile);
+    } else {
+        mp_point_tile(J, lt);
+    }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(MP_THREADS) mp_k_batch(const MPJob *__restrict__ jobs, int njobs,
+                                                         int *err)
+{
+    const int t = blockIdx.x;
+    const int j = mp_find_job(jobs, njobs, t);
+    const MPJob &J = jobs[j];
+    const int lt = t - J.tile0;
+    if (lt >= J.ntiles) return;
+    mp_run_tile<KIND>(J, lt, true, err);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(MP_THREADS) mp_k_single(const __grid_constant__ MPJob job, int *err)
+{
+    mp_run_tile<KIND>(job, blockIdx.x, false, err);
+}
+
+// In-place channel-agnostic pointwise list (brightness, gamma) over a flat
+// float buffer: float4 body plus scalar tail.
+__global__ void __launch_bounds__(MP_THREADS) mp_k_flat(float *__restrict__ data, size_t n,
+                                                        const __grid_constant__ PwList L)
+{
+    const size_t n4 = n / 4;
+    float4 *d4 = reinterpret_cast<float4 *>(data);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 q = d4[i];
+        float v0[4] = {q.x, 0.f, 0.f, 0.f}, v1[4] = {q.y, 0.f, 0.f, 0.f};
+        float v2[4] = {q.z, 0.f, 0.f, 0.f}, v3[4] = {q.w, 0.f, 0.f, 0.f};
+        mp_pw_apply(L, v0, 1);
+        mp_pw_apply(L, v1, 1);
+        mp_pw_apply(L, v2, 1);
+        mp_pw_apply(L, v3, 1);
+        d4[i] = make_float4(v0[0], v1[0], v2[0], v3[0]);
+    }
+    const size_t tail = n4 * 4 + blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (tail < n) {
+        float v[4] = {data[tail], 0.f, 0.f, 0.f};
+        mp_pw_apply(L, v, 1);
+        data[tail] = v[0];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+static MPStatus mp_prepare_smem(const void *fn, size_t smem)
+{
+    if (smem > 48 * 1024) {
+        cudaError_t e =
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return mp_cuda_status(e);
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+static int mp_current_device()
+{
+    int d = 0;
+    cudaGetDevice(&d);
+    return d;
+}
+
+MPStatus mp_launch_kind(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
+                        size_t smem, cudaStream_t s)
+{
+    if (total_tiles <= 0 || njobs <= 0) return MILLIPYDE_SUCCESS;
+    int *err = mp_device_error_word(mp_current_device());
+    const void *fn;
+    switch (kind) {
+    case MPK_GAUSS: fn = (const void *)mp_k_batch<MPK_GAUSS>; break;
+    case MPK_ROTATE: fn = (const void *)mp_k_batch<MPK_ROTATE>; break;
+    case MPK_TRANSPOSE: fn = (const void *)mp_k_batch<MPK_TRANSPOSE>; break;
+    default: fn = (const void *)mp_k_batch<MPK_POINT>; break;
+    }
+    MPStatus st = mp_prepare_smem(fn, smem);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    void *args[] = {(void *)&jobs_dev, (void *)&njobs, (void *)&err};
+    return mp_cuda_status(
+        cudaLaunchKernel(fn, dim3(total_tiles), dim3(MP_THREADS), args, smem, s));
+}
+
+MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem, cudaStream_t s)
+{
+    if (job.ntiles <= 0) return MILLIPYDE_SUCCESS;
+    int *err = mp_device_error_word(mp_current_device());
+    const void *fn;
+    switch (kind) {
+    case MPK_GAUSS: fn = (const void *)mp_k_single<MPK_GAUSS>; break;
+    case MPK_ROTATE: fn = (const void *)mp_k_single<MPK_ROTATE>; break;
+    case MPK_TRANSPOSE: fn = (const void *)mp_k_single<MPK_TRANSPOSE>; break;
+    default: fn = (const void *)mp_k_single<MPK_POINT>; break;
+    }
+    MPStatus st = mp_prepare_smem(fn, smem);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    void *args[] = {(void *)&job, (void *)&err};
+    return mp_cuda_status(
+        cudaLaunchKernel(fn, dim3(job.ntiles), dim3(MP_THREADS), args, smem, s));
+}
+
+MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s)
+{
+    if (n == 0) return MILLIPYDE_SUCCESS;
+    size_t blocks = (n / 4 + MP_THREADS - 1) / MP_THREADS;
+    if (blocks < 1) blocks = 1;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    mp_k_flat<<<(unsigned)blocks, MP_THREADS, 0, s>>>(data, n, L);
+    return mp_cuda_status(cudaGetLastError());
+}

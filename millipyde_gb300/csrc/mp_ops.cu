@@ -1,0 +1,953 @@
+// mp_ops.cu -- per-op entry points (mpimg_*) and the batch pipeline planner.
+//
+// A pipeline (or a single op) is lowered per image into SEGMENTS.  A segment
+// is one kernel launch kind (POINT, GAUSS, ROTATE, TRANSPOSE) with a
+// pointwise prologue, a pointwise epilogue and an optional fliplr output map:
+//   - pointwise ops (rgb2grey, brightness, adjust_gamma, colorize) join the
+//     prologue of a segment that has no core yet, else its epilogue;
+//   - fliplr sets the output map (pointwise ops commute with it);
+//   - gaussian / rotate / transpose become the core of the current segment if
+//     it has none and no flip yet, else they start a new segment.
+// The reference applied each stage as a separate kernel with a fresh
+// allocation and a stream sync in between (src/gpupipeline.c:373-397,
+// src/millipyde_image.cpp:859-1142); here a 4-stage pipeline such as
+// grey -> gaussian -> rotate -> gamma is two launches for the whole batch.
+#include <math.h>
+#include <string.h>
+#include <stdlib.h>
+#include <algorithm>
+#include <vector>
+
+#include "mp_internal.cuh"
+
+// Reference degree->radian constant (src/millipyde_image.cpp:702).
+#define MP_DEG2RAD 0.01745329252
+
+// Intermediate bytes a chunk of a fused batch may hold, so that the
+// intermediates written by one segment are still in L2 (129 MB on GB300)
+// when the next segment reads them.
+#define MP_L2_CHUNK_BYTES (48u << 20)
+
+struct ROp {
+    int op;
+    double p[3];
+};
+
+struct Seg {
+    int kind;
+    PwList pro, epi;
+    int flip;
+    int core_op;
+    double core_p[3];
+    int cin, cmid, cout;
+    int hin, win, hout, wout;
+};
+
+static bool mp_is_pointwise(int op)
+{
+    return op == MP_OP_RGB2GREY || op == MP_OP_BRIGHTNESS || op == MP_OP_ADJUST_GAMMA ||
+           op == MP_OP_COLORIZE;
+}
+
+static int mp_round16(long long v) { return (int)((v + 15) / 16 * 16); }
+
+// ---------------------------------------------------------------------------
+// Parameter validation and resolution
+// ---------------------------------------------------------------------------
+static MPStatus mp_check_op(int op, const double *p)
+{
+    switch (op) {
+    case MP_OP_RGB2GREY:
+    case MP_OP_TRANSPOSE:
+    case MP_OP_FLIPLR: return MILLIPYDE_SUCCESS;
+    case MP_OP_GAUSSIAN:
+        if (!(p[0] > 0.0) || !isfinite(p[0])) return MP_ERROR_INVALID_ARGS;
+        if (ceil(3.0 * p[0]) > MP_MAX_RADIUS) return MP_ERROR_TOO_LARGE;
+        return MILLIPYDE_SUCCESS;
+    case MP_OP_ROTATE:
+    case MP_OP_BRIGHTNESS: return isfinite(p[0]) ? MILLIPYDE_SUCCESS : MP_ERROR_INVALID_ARGS;
+    case MP_OP_ADJUST_GAMMA:
+        return (isfinite(p[0]) && isfinite(p[1])) ? MILLIPYDE_SUCCESS : MP_ERROR_INVALID_ARGS;
+    case MP_OP_COLORIZE:
+        return (p[0] >= 0 && p[1] >= 0 && p[2] >= 0 && isfinite(p[0]) && isfinite(p[1]) &&
+                isfinite(p[2]))
+                   ? MILLIPYDE_SUCCESS
+                   : MP_ERROR_INVALID_ARGS;
+    default: return MP_ERROR_BAD_DESCRIPTOR;
+    }
+}
+
+static MPStatus mp_resolve_image(const MPStage *stages, int nstages, uint64_t seed, uint64_t index,
+                                 std::vector<ROp> &ops, double *params_out)
+{
+    ops.clear();
+    for (int s = 0; s < nstages; ++s) {
+        const MPStage &st = stages[s];
+        ROp r;
+        r.op = st.op;
+        for (int k = 0; k < 3; ++k) {
+            if (st.random) {
+                const double u = mp_counter_uniform(seed, index, (uint32_t)s, (uint32_t)k);
+                r.p[k] = st.lo[k] + u * (st.hi[k] - st.lo[k]);
+            } else {
+                r.p[k] = st.lo[k];
+            }
+        }
+        bool run = true;
+        if (st.probability > 0.0 && st.probability < 1.0)
+            run = mp_counter_uniform(seed, index, (uint32_t)s, 3u) <= st.probability;
+        if (params_out) {
+            for (int k = 0; k < 3; ++k) params_out[s * 4 + k] = r.p[k];
+            params_out[s * 4 + 3] = run ? 1.0 : 0.0;
+        }
+        if (!run) continue;
+        MPStatus c = mp_check_op(r.op, r.p);
+        if (c != MILLIPYDE_SUCCESS) return c;
+        ops.push_back(r);
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Segmentation
+// ---------------------------------------------------------------------------
+static void mp_pw_push(PwList &L, const ROp &r)
+{
+    PwOp o;
+    o.op = r.op;
+    o.p0 = (float)r.p[0];
+    o.p1 = (float)(r.op == MP_OP_ADJUST_GAMMA ? r.p[1] : r.p[1]);
+    o.p2 = (float)r.p[2];
+    L.op[L.n++] = o;
+}
+
+static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
+                           std::vector<Seg> &segs)
+{
+    segs.clear();
+    Seg cur;
+    memset(&cur, 0, sizeof(cur));
+    cur.kind = MPK_POINT;
+    cur.core_op = MP_OP_NONE;
+    cur.cin = cur.cmid = cur.cout = cin;
+    cur.hin = cur.hout = h;
+    cur.win = cur.wout = w;
+    int c = cin;
+    for (const ROp &r : ops) {
+        if (mp_is_pointwise(r.op)) {
+            // identity cases: grey of a 1-channel image, colorize of a grey image
+            if (r.op == MP_OP_RGB2GREY && c < 3) continue;
+            if (r.op == MP_OP_COLORIZE && c < 3) continue;
+            const bool to_pro = (cur.core_op == MP_OP_NONE && !cur.flip);
+            PwList &L = to_pro ? cur.pro : cur.epi;
+            if (L.n >= MP_MAX_PW) {
+                // list full: close this segment and continue in a fresh one
+                segs.push_back(cur);
+                Seg nx;
+                memset(&nx, 0, sizeof(nx));
+                nx.kind = MPK_POINT;
+                nx.cin = nx.cmid = nx.cout = c;
+                nx.hin = nx.hout = cur.hout;
+                nx.win = nx.wout = cur.wout;
+                cur = nx;
+                mp_pw_push(cur.pro, r);
+            } else {
+                mp_pw_push(L, r);
+            }
+            if (r.op == MP_OP_RGB2GREY) c = 1;
+            if (cur.core_op == MP_OP_NONE && !cur.flip && to_pro) cur.cmid = c;
+            cur.cout = c;
+            continue;
+        }
+        if (r.op == MP_OP_FLIPLR) {
+            cur.flip ^= 1;
+            continue;
+        }
+        // core op
+        if (!(cur.core_op == MP_OP_NONE && !cur.flip)) {
+            segs.push_back(cur);
+            Seg nx;
+            memset(&nx, 0, sizeof(nx));
+            nx.cin = nx.cmid = nx.cout = c;
+            nx.hin = nx.hout = cur.hout;
+            nx.win = nx.wout = cur.wout;
+            cur = nx;
+        }
+        cur.core_op = r.op;
+        cur.core_p[0] = r.p[0];
+        cur.core_p[1] = r.p[1];
+        cur.core_p[2] = r.p[2];
+        cur.cmid = c;
+        cur.cout = c;
+        if (r.op == MP_OP_GAUSSIAN) cur.kind = MPK_GAUSS;
+        else if (r.op == MP_OP_ROTATE) cur.kind = MPK_ROTATE;
+        else {
+            cur.kind = MPK_TRANSPOSE;
+            std::swap(cur.hout, cur.wout);
+        }
+    }
+    segs.push_back(cur);
+    return MILLIPYDE_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Job construction
+// ---------------------------------------------------------------------------
+static int mp_max_smem_optin()
+{
+    static int v = 0;
+    if (!v) {
+        int d = 0;
+        cudaGetDevice(&d);
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, d) != cudaSuccess ||
+            v <= 0) {
+            cudaGetLastError();
+            v = 227 * 1024;
+        }
+    }
+    return v;
+}
+
+// Tile (tw, th) for a GAUSS launch: the largest candidate whose shared memory
+// lets two CTAs share an SM, else the largest that fits at all.
+static void mp_gauss_tiles(int r, int cin, int cmid, int has_pro, int *tw, int *th)
+{
+    static const int grey[][2] = {{128, 32}, {64, 32}, {64, 16}, {32, 16}, {32, 8}, {16, 8}, {8, 8}};
+    static const int colr[][2] = {{64, 32}, {32, 32}, {32, 16}, {16, 16}, {16, 8}, {8, 8}};
+    const int(*cand)[2] = cmid == 1 ? grey : colr;
+    const int nc = cmid == 1 ? 7 : 6;
+    const size_t lim = (size_t)mp_max_smem_optin();
+    for (int pass = 0; pass < 2; ++pass) {
+        const size_t budget = pass == 0 ? lim / 2 - 1024 : lim;
+        for (int i = 0; i < nc; ++i) {
+            if (cand[i][1] + 2 * r > 256) continue;
+            if (mp_gauss_smem_bytes(cand[i][0], cand[i][1], r, cin, cmid, has_pro) <= budget) {
+                *tw = cand[i][0];
+                *th = cand[i][1];
+                return;
+            }
+        }
+    }
+    *tw = 8;
+    *th = 8;
+}
+
+static MPStatus mp_fill_job(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out, int tw,
+                            int th)
+{
+    memset(&J, 0, sizeof(J));
+    J.src = (const float *)in.data;
+    J.dst = (float *)out.data;
+    J.h = in.height;
+    J.w = in.width;
+    J.ho = out.height;
+    J.wo = out.width;
+    J.src_pitch = in.pitch / 4;
+    J.dst_pitch = out.pitch / 4;
+    J.cin = sg.cin;
+    J.cmid = sg.cmid;
+    J.cout = sg.cout;
+    J.flip = sg.flip;
+    J.pro = sg.pro;
+    J.epi = sg.epi;
+    switch (sg.kind) {
+    case MPK_POINT:
+        J.tiles_x = (in.width + 255) / 256;
+        J.ntiles = J.tiles_x * ((in.height + 3) / 4);
+        break;
+    case MPK_ROTATE: {
+        const double th_r = sg.core_p[0] * MP_DEG2RAD;
+        const double scale = (double)(1LL << (MP_FIX_FRAC - 1));
+        J.cosq = llround(cos(th_r) * scale);
+        J.sinq = llround(sin(th_r) * scale);
+        J.tiles_x = (out.width + 31) / 32;
+        J.ntiles = J.tiles_x * ((out.height + 31) / 32);
+        break;
+    }
+    case MPK_TRANSPOSE:
+        J.tiles_x = (in.width + 31) / 32;
+        J.ntiles = J.tiles_x * ((in.height + 31) / 32);
+        break;
+    case MPK_GAUSS: {
+        const double sigma = sg.core_p[0];
+        const int r = (int)ceil(3.0 * sigma);
+        if (r < 1 || r > MP_MAX_RADIUS) return MP_ERROR_TOO_LARGE;
+        J.radius = r;
+        double e[MP_MAX_TAPS], sum = 0.0;
+        for (int k = -r; k <= r; ++k) {
+            e[k + r] = exp(-(double)(k * k) / (2.0 * sigma * sigma));
+            sum += e[k + r];
+        }
+        for (int k = 0; k < 2 * r + 1; ++k) J.wts[k] = (float)(e[k] / sum);
+        J.tw = tw;
+        J.th = th;
+        J.tiles_x = (in.width + tw - 1) / tw;
+        J.ntiles = J.tiles_x * ((in.height + th - 1) / th);
+        J.use_tma = 0;
+        if ((in.pitch % 16) == 0 && (((uintptr_t)in.data) % 16) == 0 && in.width > 0 &&
+            in.height > 0) {
+            mp_encode_tiled_fn enc = mp_get_encode_tiled();
+            if (enc) {
+                cuuint64_t gdim[2] = {(cuuint64_t)in.width * (cuuint64_t)sg.cin,
+                                      (cuuint64_t)in.height};
+                cuuint64_t gstr[1] = {(cuuint64_t)in.pitch};
+                cuuint32_t box[2] = {64u, (cuuint32_t)(th + 2 * r)};
+                cuuint32_t es[2] = {1u, 1u};
+                CUresult cr = enc(&J.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)in.data, gdim,
+                                  gstr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                if (cr == CUDA_SUCCESS) J.use_tma = 1;
+            }
+        }
+        break;
+    }
+    default: return MP_ERROR_BAD_DESCRIPTOR;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+static void mp_seg_tiles(const Seg &sg, int *tw, int *th)
+{
+    *tw = *th = 0;
+    if (sg.kind == MPK_GAUSS) {
+        const int r = (int)ceil(3.0 * sg.core_p[0]);
+        mp_gauss_tiles(r, sg.cin, sg.cmid, sg.pro.n > 0, tw, th);
+    }
+}
+
+static size_t mp_seg_smem(const Seg &sg, int tw, int th)
+{
+    if (sg.kind != MPK_GAUSS) return 0;
+    const int r = (int)ceil(3.0 * sg.core_p[0]);
+    return mp_gauss_smem_bytes(tw, th, r, sg.cin, sg.cmid, sg.pro.n > 0);
+}
+
+// Runs one segment on one image with the job passed by value.
+static MPStatus mp_run_segment_single(const Seg &sg, const MPImage &in, const MPImage &out,
+                                      cudaStream_t s)
+{
+    int tw, th;
+    mp_seg_tiles(sg, &tw, &th);
+    MPJob J;
+    MPStatus st = mp_fill_job(J, sg, in, out, tw, th);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    return mp_launch_single(sg.kind, J, mp_seg_smem(sg, tw, th), s);
+}
+
+// ---------------------------------------------------------------------------
+// Plans: host-resolved job tables + launches (capturable in a CUDA graph).
+// ---------------------------------------------------------------------------
+struct MPLaunch {
+    int kind;
+    size_t job_off;
+    int njobs;
+    int total_tiles;
+    size_t smem;
+};
+
+struct MPPlanImpl {
+    std::vector<MPLaunch> launches;
+    MPJob *jobs_dev = nullptr;
+    void *scratch = nullptr;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+};
+
+static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage *in,
+                              const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
+                              cudaStream_t s, MPPlanImpl *P)
+{
+    if (nimgs < 0 || nstages < 0 || (nimgs > 0 && (!in || !out)) || (nstages > 0 && !stages))
+        return MP_ERROR_BAD_DESCRIPTOR;
+    // 1. resolve + segment every image
+    std::vector<std::vector<Seg>> segs(nimgs);
+    std::vector<ROp> ops;
+    for (int i = 0; i < nimgs; ++i) {
+        if (in[i].height < 0 || in[i].width < 0 || in[i].pitch < 0 || (in[i].pitch % 4) ||
+            (in[i].channels != 1 && in[i].channels != 3 && in[i].channels != 4))
+            return MP_ERROR_BAD_DESCRIPTOR;
+        if ((long long)in[i].width * in[i].channels * 4 > in[i].pitch && in[i].height > 0)
+            return MP_ERROR_BAD_DESCRIPTOR;
+        MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, nullptr);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        mp_segment(ops, in[i].channels, in[i].height, in[i].width, segs[i]);
+        const Seg &last = segs[i].back();
+        if (!out[i].data && (long long)last.hout * last.wout > 0) return MP_ERROR_NULL_DATA;
+        if (out[i].height != last.hout || out[i].width != last.wout ||
+            out[i].channels != last.cout || out[i].pitch < last.wout * last.cout * 4 ||
+            (out[i].pitch % 4))
+            return MP_ERROR_BAD_DESCRIPTOR;
+    }
+    // 2. group images by their sequence of segment kinds (keeps batch order
+    //    within a group), then chunk each group so intermediates stay in L2.
+    std::vector<int> order(nimgs);
+    for (int i = 0; i < nimgs; ++i) order[i] = i;
+    auto sig_less = [&](int a, int b) {
+        const auto &A = segs[a], &B = segs[b];
+        if (A.size() != B.size()) return A.size() < B.size();
+        for (size_t k = 0; k < A.size(); ++k)
+            if (A[k].kind != B[k].kind) return A[k].kind < B[k].kind;
+        return a < b;
+    };
+    std::sort(order.begin(), order.end(), sig_less);
+
+    struct Chunk { std::vector<int> imgs; };
+    std::vector<Chunk> chunks;
+    size_t scratch_need = 0;
+    {
+        size_t i = 0;
+        while (i < order.size()) {
+            Chunk ch;
+            size_t bytes = 0;
+            const auto &sig0 = segs[order[i]];
+            while (i < order.size()) {
+                const auto &sg = segs[order[i]];
+                bool same = sg.size() == sig0.size();
+                for (size_t k = 0; same && k < sg.size(); ++k) same = sg[k].kind == sig0[k].kind;
+                if (!same) break;
+                size_t b = 0;
+                for (size_t k = 0; k + 1 < sg.size(); ++k)
+                    b += (size_t)sg[k].hout * mp_round16((long long)sg[k].wout * sg[k].cout * 4);
+                if (!ch.imgs.empty() && bytes + b > MP_L2_CHUNK_BYTES) break;
+                bytes += b;
+                ch.imgs.push_back(order[i]);
+                ++i;
+            }
+            scratch_need = std::max(scratch_need, bytes);
+            chunks.push_back(ch);
+        }
+    }
+    // 3. scratch for intermediates (reused by every chunk, stream-ordered)
+    MPStatus st = mp_malloc_async(&P->scratch, scratch_need, s);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    // 4. jobs
+    std::vector<MPJob> jobs;
+    for (const Chunk &ch : chunks) {
+        const size_t nseg = segs[ch.imgs[0]].size();
+        // intermediate images of this chunk
+        std::vector<std::vector<MPImage>> inter(ch.imgs.size(), std::vector<MPImage>(nseg));
+        size_t off = 0;
+        for (size_t q = 0; q < ch.imgs.size(); ++q) {
+            const auto &sg = segs[ch.imgs[q]];
+            for (size_t k = 0; k + 1 < nseg; ++k) {
+                MPImage m;
+                m.height = sg[k].hout;
+                m.width = sg[k].wout;
+                m.channels = sg[k].cout;
+                m.pitch = mp_round16((long long)m.width * m.channels * 4);
+                m.data = (char *)P->scratch + off;
+                off += (size_t)m.height * m.pitch;
+                inter[q][k] = m;
+            }
+        }
+        for (size_t k = 0; k < nseg; ++k) {
+            // uniform tile geometry for this launch
+            int kind = segs[ch.imgs[0]][k].kind;
+            int tw = 0, th = 0;
+            size_t smem = 0;
+            if (kind == MPK_GAUSS) {
+                int rmax = 0, cinm = 1, cmidm = 1, pro = 0;
+                for (int img : ch.imgs) {
+                    const Seg &sg = segs[img][k];
+                    rmax = std::max(rmax, (int)ceil(3.0 * sg.core_p[0]));
+                    cinm = std::max(cinm, sg.cin);
+                    cmidm = std::max(cmidm, sg.cmid);
+                    pro |= sg.pro.n > 0;
+                }
+                mp_gauss_tiles(rmax, cinm, cmidm, pro, &tw, &th);
+                smem = mp_gauss_smem_bytes(tw, th, rmax, cinm, cmidm, pro);
+            }
+            MPLaunch L;
+            L.kind = kind;
+            L.job_off = jobs.size();
+            L.njobs = 0;
+            L.total_tiles = 0;
+            L.smem = smem;
+            for (size_t q = 0; q < ch.imgs.size(); ++q) {
+                const int img = ch.imgs[q];
+                const Seg &sg = segs[img][k];
+                const MPImage &src = (k == 0) ? in[img] : inter[q][k - 1];
+                const MPImage &dst = (k + 1 == nseg) ? out[img] : inter[q][k];
+                MPJob J;
+                st = mp_fill_job(J, sg, src, dst, tw, th);
+                if (st != MILLIPYDE_SUCCESS) return st;
+                if (J.ntiles <= 0) continue;
+                if ((long long)L.total_tiles + J.ntiles > 0x7fffffffLL) return MP_ERROR_TOO_LARGE;
+                J.tile0 = L.total_tiles;
+                L.total_tiles += J.ntiles;
+                jobs.push_back(J);
+                L.njobs++;
+            }
+            if (L.njobs > 0) P->launches.push_back(L);
+        }
+    }
+    if (!jobs.empty()) {
+        st = mp_malloc_async((void **)&P->jobs_dev, jobs.size() * sizeof(MPJob), s);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        MP_CUDA_TRY(cudaMemcpyAsync(P->jobs_dev, jobs.data(), jobs.size() * sizeof(MPJob),
+                                    cudaMemcpyHostToDevice, s));
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
+{
+    for (const MPLaunch &L : P->launches) {
+        MPStatus st = mp_launch_kind(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles,
+                                     L.smem, s);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+static void mp_plan_free(MPPlanImpl *P, cudaStream_t s)
+{
+    mp_free_async(P->jobs_dev, s);
+    mp_free_async(P->scratch, s);
+    P->jobs_dev = nullptr;
+    P->scratch = nullptr;
+}
+
+extern "C" {
+
+MPStatus mpk_plan_create(const MPStage *stages, int nstages, const MPImage *in, const MPImage *out,
+                         int nimgs, uint64_t seed, uint64_t index0, void *stream, MPPlan **plan)
+{
+    if (!plan) return MP_ERROR_INVALID_ARGS;
+    *plan = nullptr;
+    MPPlanImpl *P = new (std::nothrow) MPPlanImpl();
+    if (!P) return MP_ERROR_OUT_OF_MEMORY;
+    cudaGetDevice(&P->device);
+    P->stream = (cudaStream_t)stream;
+    MPStatus st = mp_plan_build(stages, nstages, in, out, nimgs, seed, index0, P->stream, P);
+    if (st != MILLIPYDE_SUCCESS) {
+        mp_plan_free(P, P->stream);
+        delete P;
+        return st;
+    }
+    *plan = (MPPlan *)P;
+    return MILLIPYDE_SUCCESS;
+}
+
+MPStatus mpk_plan_launch(MPPlan *plan, void *stream)
+{
+    if (!plan) return MP_ERROR_INVALID_ARGS;
+    return mp_plan_launch((MPPlanImpl *)plan, (cudaStream_t)stream);
+}
+
+int mpk_plan_num_launches(const MPPlan *plan)
+{
+    return plan ? (int)((const MPPlanImpl *)plan)->launches.size() : 0;
+}
+
+MPStatus mpk_plan_destroy(MPPlan *plan)
+{
+    if (!plan) return MILLIPYDE_SUCCESS;
+    MPPlanImpl *P = (MPPlanImpl *)plan;
+    mp_plan_free(P, P->stream);
+    delete P;
+    return MILLIPYDE_SUCCESS;
+}
+
+MPStatus mpk_pipeline_resolve(const MPStage *stages, int nstages, int nimgs, uint64_t seed,
+                              uint64_t index0, double *params)
+{
+    if (nimgs < 0 || nstages < 0 || !params) return MP_ERROR_INVALID_ARGS;
+    std::vector<ROp> ops;
+    for (int i = 0; i < nimgs; ++i) {
+        MPStatus st =
+            mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, params + (size_t)i * nstages * 4);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+MPStatus mpk_pipeline_shapes(const MPStage *stages, int nstages, const MPImage *in, MPImage *out,
+                             int nimgs, uint64_t seed, uint64_t index0)
+{
+    if (nimgs < 0 || nstages < 0 || (nimgs > 0 && (!in || !out))) return MP_ERROR_INVALID_ARGS;
+    std::vector<ROp> ops;
+    std::vector<Seg> segs;
+    for (int i = 0; i < nimgs; ++i) {
+        if (in[i].channels != 1 && in[i].channels != 3 && in[i].channels != 4)
+            return MP_ERROR_BAD_DESCRIPTOR;
+        MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, nullptr);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        mp_segment(ops, in[i].channels, in[i].height, in[i].width, segs);
+        const Seg &l = segs.back();
+        out[i].height = l.hout;
+        out[i].width = l.wout;
+        out[i].channels = l.cout;
+        out[i].pitch = mp_round16((long long)l.wout * l.cout * 4);
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+MPStatus mpk_pipeline_run(const MPStage *stages, int nstages, const MPImage *in, MPImage *out,
+                          int nimgs, uint64_t seed, uint64_t index0, void *stream)
+{
+    MPPlan *p = nullptr;
+    MPStatus st = mpk_plan_create(stages, nstages, in, out, nimgs, seed, index0, stream, &p);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    st = mpk_plan_launch(p, stream);
+    mpk_plan_destroy(p);
+    return st;
+}
+
+}  // extern "C"
+
+// Plain per-op path: one launch per stage and image, a fresh pool buffer per
+// stage (what the reference's Pipeline did, minus its per-stage host sync).
+static MPStatus mp_run_ops_unfused(const std::vector<ROp> &ops, const MPImage &in,
+                                   const MPImage &out, cudaStream_t s)
+{
+    MPImage cur = in;
+    void *owned = nullptr;
+    if (ops.empty()) {
+        std::vector<Seg> sg;
+        mp_segment(ops, in.channels, in.height, in.width, sg);
+        return mp_run_segment_single(sg[0], in, out, s);
+    }
+    for (size_t k = 0; k < ops.size(); ++k) {
+        std::vector<ROp> one(1, ops[k]);
+        std::vector<Seg> sg;
+        mp_segment(one, cur.channels, cur.height, cur.width, sg);
+        const Seg &g = sg.back();
+        MPImage nx;
+        void *buf = nullptr;
+        if (k + 1 == ops.size()) {
+            nx = out;
+        } else {
+            nx.height = g.hout;
+            nx.width = g.wout;
+            nx.channels = g.cout;
+            nx.pitch = mp_round16((long long)nx.width * nx.channels * 4);
+            MPStatus st = mp_malloc_async(&buf, (size_t)nx.height * nx.pitch, s);
+            if (st != MILLIPYDE_SUCCESS) { mp_free_async(owned, s); return st; }
+            nx.data = buf;
+        }
+        MPStatus st = mp_run_segment_single(g, cur, nx, s);
+        mp_free_async(owned, s);
+        owned = buf;
+        if (st != MILLIPYDE_SUCCESS) { mp_free_async(owned, s); return st; }
+        cur = nx;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_pipeline_run_unfused(const MPStage *stages, int nstages, const MPImage *in,
+                                             MPImage *out, int nimgs, uint64_t seed,
+                                             uint64_t index0, void *stream)
+{
+    if (nimgs < 0 || nstages < 0 || (nimgs > 0 && (!in || !out))) return MP_ERROR_INVALID_ARGS;
+    std::vector<ROp> ops;
+    for (int i = 0; i < nimgs; ++i) {
+        MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, nullptr);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        st = mp_run_ops_unfused(ops, in[i], out[i], (cudaStream_t)stream);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Per-op entry points on MPObjData (src/millipyde_image.cpp:530-717).
+// ---------------------------------------------------------------------------
+#define MP_NPY_FLOAT32 11
+
+// Describes a float32 image object; MP_ERROR_UNSUPPORTED_TYPE for others.
+static MPStatus mp_obj_image(const MPObjData *o, MPImage *m)
+{
+    if (!o) return MP_ERROR_INVALID_ARGS;
+    if (o->ndims != 2 && o->ndims != 3) return MP_ERROR_UNSUPPORTED_DIMS;
+    if (o->type != MP_NPY_FLOAT32) return MP_ERROR_UNSUPPORTED_TYPE;
+    m->height = o->dims[0];
+    m->width = o->dims[1];
+    m->channels = o->ndims == 3 ? o->dims[2] : 1;
+    if (m->channels != 1 && m->channels != 3 && m->channels != 4) return MP_ERROR_UNSUPPORTED_TYPE;
+    m->pitch = o->dims[o->ndims];
+    m->data = o->device_data;
+    if ((long long)m->height * m->width > 0 && !m->data) return MP_ERROR_NULL_DATA;
+    return MILLIPYDE_SUCCESS;
+}
+
+// Points obj at a new float32 image buffer of the given geometry.
+static MPStatus mp_obj_set_image(MPObjData *o, void *data, int h, int w, int c, int pitch)
+{
+    const int nd = (c == 1) ? 2 : 3;
+    int *dims = (int *)malloc(sizeof(int) * 2 * nd);
+    if (!dims) return MP_ERROR_OUT_OF_MEMORY;
+    dims[0] = h;
+    dims[1] = w;
+    if (nd == 3) dims[2] = c;
+    dims[nd] = pitch;
+    dims[nd + 1] = (nd == 3) ? c * 4 : 4;
+    if (nd == 3) dims[nd + 2] = 4;
+    if (o->device_data && o->device_data != data)
+        mp_free_async(o->device_data, (cudaStream_t)o->stream);
+    free(o->dims);
+    o->dims = dims;
+    o->ndims = nd;
+    o->device_data = data;
+    o->type = MP_NPY_FLOAT32;
+    o->nbytes = (size_t)h * pitch;
+    return MILLIPYDE_SUCCESS;
+}
+
+// Runs one op on an object out of place (new pool buffer, old one freed).
+static MPStatus mp_obj_apply(MPObjData *o, int op, double p0, double p1, double p2)
+{
+    MPImage in;
+    MPStatus st = mp_obj_image(o, &in);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    ROp r;
+    r.op = op;
+    r.p[0] = p0;
+    r.p[1] = p1;
+    r.p[2] = p2;
+    st = mp_check_op(op, r.p);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    MP_CUDA_TRY(cudaSetDevice(o->mem_loc));
+    cudaStream_t s = (cudaStream_t)o->stream;
+    std::vector<ROp> ops(1, r);
+    std::vector<Seg> sg;
+    mp_segment(ops, in.channels, in.height, in.width, sg);
+    const Seg &g = sg.back();
+    // in-place fast path: channel-agnostic pointwise op on 1- or 3-channel data
+    if (g.kind == MPK_POINT && !g.flip && (op == MP_OP_BRIGHTNESS || op == MP_OP_ADJUST_GAMMA) &&
+        in.channels != 4) {
+        PwList L = g.pro;
+        return mp_launch_flat((float *)in.data, o->nbytes / 4, L, s);
+    }
+    if (g.kind == MPK_POINT && !g.flip && g.pro.n == 0 && g.epi.n == 0)
+        return MILLIPYDE_SUCCESS;   // identity (e.g. rgb2grey of a grey image)
+    MPImage out;
+    out.height = g.hout;
+    out.width = g.wout;
+    out.channels = g.cout;
+    out.pitch = mp_round16((long long)out.width * out.channels * 4);
+    void *buf = nullptr;
+    st = mp_malloc_async(&buf, (size_t)out.height * out.pitch, s);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    out.data = buf;
+    st = mp_run_segment_single(g, in, out, s);
+    if (st != MILLIPYDE_SUCCESS) {
+        mp_free_async(buf, s);
+        return st;
+    }
+    return mp_obj_set_image(o, buf, out.height, out.width, out.channels, out.pitch);
+}
+
+extern "C" {
+
+MPStatus mpimg_color_to_greyscale(MPObjData *obj_data, void *args)
+{
+    (void)args;
+    return mp_obj_apply(obj_data, MP_OP_RGB2GREY, 0, 0, 0);
+}
+
+MPStatus mpimg_transpose(MPObjData *obj_data, void *args)
+{
+    (void)args;
+    return mp_obj_apply(obj_data, MP_OP_TRANSPOSE, 0, 0, 0);
+}
+
+MPStatus mpimg_gaussian(MPObjData *obj_data, void *args)
+{
+    if (!args) return MP_ERROR_INVALID_ARGS;
+    return mp_obj_apply(obj_data, MP_OP_GAUSSIAN, ((GaussianArgs *)args)->sigma, 0, 0);
+}
+
+MPStatus mpimg_fliplr(MPObjData *obj_data, void *args)
+{
+    (void)args;
+    return mp_obj_apply(obj_data, MP_OP_FLIPLR, 0, 0, 0);
+}
+
+MPStatus mpimg_rotate(MPObjData *obj_data, void *args)
+{
+    if (!args) return MP_ERROR_INVALID_ARGS;
+    return mp_obj_apply(obj_data, MP_OP_ROTATE, ((RotateArgs *)args)->angle, 0, 0);
+}
+
+MPStatus mpimg_brightness(MPObjData *obj_data, void *args)
+{
+    if (!args) return MP_ERROR_INVALID_ARGS;
+    return mp_obj_apply(obj_data, MP_OP_BRIGHTNESS, ((BrightnessArgs *)args)->delta, 0, 0);
+}
+
+MPStatus mpimg_colorize(MPObjData *obj_data, void *args)
+{
+    if (!args) return MP_ERROR_INVALID_ARGS;
+    const ColorizeArgs *a = (const ColorizeArgs *)args;
+    return mp_obj_apply(obj_data, MP_OP_COLORIZE, a->r_mult, a->g_mult, a->b_mult);
+}
+
+MPStatus mpimg_adjust_gamma(MPObjData *obj_data, void *args)
+{
+    if (!args) return MP_ERROR_INVALID_ARGS;
+    const GammaArgs *a = (const GammaArgs *)args;
+    return mp_obj_apply(obj_data, MP_OP_ADJUST_GAMMA, a->gamma, a->gain, 0);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Object-level batches for Pipeline.run and Generator.
+// ---------------------------------------------------------------------------
+static MPStatus mp_obj_apply_resolved(MPObjData *o, const std::vector<ROp> &ops)
+{
+    for (const ROp &r : ops) {
+        MPStatus st = mp_obj_apply(o, r.op, r.p[0], r.p[1], r.p[2]);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+// One batch over distinct objects.
+static MPStatus mp_run_objects_once(const MPStage *stages, int nstages, MPObjData **objs,
+                                    const std::vector<int> &idx, uint64_t seed, uint64_t index0,
+                                    int fused)
+{
+    const int n = (int)idx.size();
+    if (n == 0) return MILLIPYDE_SUCCESS;
+    bool all_float = true;
+    std::vector<MPImage> in(n), out(n);
+    for (int q = 0; q < n; ++q)
+        if (mp_obj_image(objs[idx[q]], &in[q]) != MILLIPYDE_SUCCESS) all_float = false;
+    if (!all_float) {
+        std::vector<ROp> ops;
+        for (int q = 0; q < n; ++q) {
+            MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)idx[q], ops, nullptr);
+            if (st != MILLIPYDE_SUCCESS) return st;
+            st = mp_obj_apply_resolved(objs[idx[q]], ops);
+            if (st != MILLIPYDE_SUCCESS) return st;
+        }
+        return MILLIPYDE_SUCCESS;
+    }
+    MPObjData *o0 = objs[idx[0]];
+    for (int q = 1; q < n; ++q)
+        if (objs[idx[q]]->mem_loc != o0->mem_loc) return MP_ERROR_BAD_DESCRIPTOR;
+    MP_CUDA_TRY(cudaSetDevice(o0->mem_loc));
+    cudaStream_t s = (cudaStream_t)o0->stream;
+    for (int q = 1; q < n; ++q)
+        if (objs[idx[q]]->stream != o0->stream) cudaStreamSynchronize((cudaStream_t)objs[idx[q]]->stream);
+    // shapes per image (each image's own index for random draws)
+    for (int q = 0; q < n; ++q) {
+        MPStatus st = mpk_pipeline_shapes(stages, nstages, &in[q], &out[q], 1, seed,
+                                          index0 + (uint64_t)idx[q]);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    MPStatus st = MILLIPYDE_SUCCESS;
+    for (int q = 0; q < n && st == MILLIPYDE_SUCCESS; ++q)
+        st = mp_malloc_async(&out[q].data, (size_t)out[q].height * out[q].pitch, s);
+    if (st == MILLIPYDE_SUCCESS) {
+        // images keep their list index for random draws: run per contiguous index run
+        bool contiguous = true;
+        for (int q = 1; q < n; ++q) contiguous &= idx[q] == idx[q - 1] + 1;
+        if (contiguous) {
+            st = fused ? mpk_pipeline_run(stages, nstages, in.data(), out.data(), n, seed,
+                                          index0 + (uint64_t)idx[0], s)
+                       : mpk_pipeline_run_unfused(stages, nstages, in.data(), out.data(), n, seed,
+                                                  index0 + (uint64_t)idx[0], s);
+        } else {
+            for (int q = 0; q < n && st == MILLIPYDE_SUCCESS; ++q)
+                st = fused ? mpk_pipeline_run(stages, nstages, &in[q], &out[q], 1, seed,
+                                              index0 + (uint64_t)idx[q], s)
+                           : mpk_pipeline_run_unfused(stages, nstages, &in[q], &out[q], 1, seed,
+                                                      index0 + (uint64_t)idx[q], s);
+        }
+    }
+    if (st != MILLIPYDE_SUCCESS) {
+        for (int q = 0; q < n; ++q) mp_free_async(out[q].data, s);
+        return st;
+    }
+    for (int q = 0; q < n; ++q) {
+        MPObjData *o = objs[idx[q]];
+        o->stream = (void *)s;
+        st = mp_obj_set_image(o, out[q].data, out[q].height, out[q].width, out[q].channels,
+                              out[q].pitch);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_pipeline_run_objects(const MPStage *stages, int nstages, MPObjData **objs,
+                                             int nobjs, uint64_t seed, uint64_t index0, int fused)
+{
+    if (nobjs < 0 || (nobjs > 0 && !objs) || nstages < 0) return MP_ERROR_INVALID_ARGS;
+    // rounds: the k-th occurrence of each object goes into round k
+    std::vector<int> round(nobjs, 0);
+    int nrounds = nobjs > 0 ? 1 : 0;
+    for (int i = 0; i < nobjs; ++i) {
+        if (!objs[i]) return MP_ERROR_INVALID_ARGS;
+        for (int j = 0; j < i; ++j)
+            if (objs[j] == objs[i]) round[i] = std::max(round[i], round[j] + 1);
+        nrounds = std::max(nrounds, round[i] + 1);
+    }
+    for (int r = 0; r < nrounds; ++r) {
+        std::vector<int> idx;
+        for (int i = 0; i < nobjs; ++i)
+            if (round[i] == r) idx.push_back(i);
+        MPStatus st = mp_run_objects_once(stages, nstages, objs, idx, seed, index0, fused);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_pipeline_produce(const MPStage *stages, int nstages, MPObjData **srcs,
+                                         MPObjData **outs, int n, uint64_t seed, uint64_t index0)
+{
+    if (n < 0 || (n > 0 && (!srcs || !outs))) return MP_ERROR_INVALID_ARGS;
+    if (n == 0) return MILLIPYDE_SUCCESS;
+    std::vector<MPImage> in(n), out(n);
+    bool all_float = true;
+    for (int i = 0; i < n; ++i)
+        if (mp_obj_image(srcs[i], &in[i]) != MILLIPYDE_SUCCESS) all_float = false;
+    if (!all_float) {
+        std::vector<ROp> ops;
+        for (int i = 0; i < n; ++i) {
+            MPObjData *c = mpobj_clone_data(srcs[i], srcs[i]->mem_loc, 0);
+            if (!c) return MP_ERROR_CUDA;
+            MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, nullptr);
+            if (st == MILLIPYDE_SUCCESS) st = mp_obj_apply_resolved(c, ops);
+            if (st != MILLIPYDE_SUCCESS) {
+                mpobj_dealloc_device_data(c);
+                free(c);
+                for (int k = 0; k < i; ++k) mpobj_dealloc_device_data(outs[k]);
+                return st;
+            }
+            *outs[i] = *c;
+            free(c);
+        }
+        return MILLIPYDE_SUCCESS;
+    }
+    const int dev = srcs[0]->mem_loc;
+    MP_CUDA_TRY(cudaSetDevice(dev));
+    cudaStream_t s = (cudaStream_t)mpdev_get_stream(dev, 0);
+    if (!s) return MP_ERROR_NO_DEVICE;
+    for (int i = 0; i < n; ++i)
+        if (srcs[i]->stream != (void *)s) cudaStreamSynchronize((cudaStream_t)srcs[i]->stream);
+    MPStatus st = mpk_pipeline_shapes(stages, nstages, in.data(), out.data(), n, seed, index0);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    for (int i = 0; i < n && st == MILLIPYDE_SUCCESS; ++i)
+        st = mp_malloc_async(&out[i].data, (size_t)out[i].height * out[i].pitch, s);
+    if (st == MILLIPYDE_SUCCESS)
+        st = mpk_pipeline_run(stages, nstages, in.data(), out.data(), n, seed, index0, s);
+    if (st != MILLIPYDE_SUCCESS) {
+        for (int i = 0; i < n; ++i) mp_free_async(out[i].data, s);
+        return st;
+    }
+    for (int i = 0; i < n; ++i) {
+        MPObjData *o = outs[i];
+        memset(o, 0, sizeof(*o));
+        o->mem_loc = dev;
+        o->stream = (void *)s;
+        o->type = MP_NPY_FLOAT32;
+        st = mp_obj_set_image(o, out[i].data, out[i].height, out[i].width, out[i].channels,
+                              out[i].pitch);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}

@@ -1,0 +1,29 @@
+"""Shared test set-up: builds the extension in-tree, registers the `gpu` marker."""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from millipyde_gb300 import _build  # noqa: E402
+
+_build.build()
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def has_gpu():
+    from millipyde_gb300 import _abi
+    return _abi.lib().mpdev_get_device_count() > 0
+
+
+@pytest.fixture(scope="session")
+def gpu():
+    if not has_gpu():
+        pytest.skip("no CUDA device")
+    return 0
