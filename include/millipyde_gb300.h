@@ -308,6 +308,26 @@ MPStatus mpk_plan_launch(MPPlan *plan, void *stream);
 int mpk_plan_num_launches(const MPPlan *plan);
 MPStatus mpk_plan_destroy(MPPlan *plan);
 
+/* Launches launches [first, first+count) of a plan only, and describes
+ * launch i (kind: 0 pointwise, 1 gaussian, 2 rotate, 3 transpose; njobs
+ * images; tiles CTAs; bytes = algorithmic bytes moved: every input pixel read
+ * once and every output pixel written once, float32). */
+MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream);
+MPStatus mpk_plan_launch_info(const MPPlan *plan, int i, int *kind, int *njobs, int *tiles,
+                              double *bytes);
+
+/* Host-buffer batch: in[i].data / out[i].data are HOST pointers and pitch the
+ * host row stride in bytes (out[i] geometry from mpk_pipeline_shapes, pitch
+ * may be changed to the packed row size).  Images move in chunks through
+ * device staging buffers: the host->device copy of chunk k+1, the kernels of
+ * chunk k and the device->host copy of chunk k-1 run concurrently on three
+ * streams.  Page-locked host memory (cudaHostAlloc / cudaHostRegister) gives
+ * the overlap; pageable memory works but serialises the copies.  Returns
+ * after the last result is on the host. */
+MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, const MPImage *in,
+                               const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
+                               void *stream);
+
 /* Object-level batch used by Pipeline.run: applies the stages in place to
  * each object (float32 images: fused path when fused != 0, else one launch
  * per stage and image; other dtypes: the per-op entry points).  Image i uses

@@ -8,8 +8,8 @@ as millipyde` is the switch.
 
 The compute path is the compiled extension `_millipyde` over the C-ABI
 library `libmillipyde_gb300.so`; there is no CPU fallback.  Importing fails
-with ImportError when the extension has not been built (call
-`millipyde_gb300._build.build()`).
+with ImportError when the extension has not been built (run
+`python millipyde_gb300/_build.py`).
 """
 from __future__ import annotations
 
@@ -33,7 +33,7 @@ try:
 except ImportError as e:  # pragma: no cover - exercised only without a build
     raise ImportError(
         "millipyde_gb300: the compiled extension is missing (%s); build it with "
-        "`python -c 'import millipyde_gb300._build as b; b.build()'`" % e
+        "`python millipyde_gb300/_build.py`" % e
     ) from e
 
 from ._io import image_from_path, images_from_path  # noqa: E402,F401

@@ -118,6 +118,11 @@ SIGNATURES = {
     "mpk_plan_launch": (_ST, [_P, _P]),
     "mpk_plan_num_launches": (C.c_int, [_P]),
     "mpk_plan_destroy": (_ST, [_P]),
+    "mpk_plan_launch_range": (_ST, [_P, C.c_int, C.c_int, _P]),
+    "mpk_plan_launch_info": (_ST, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "mpk_pipeline_run_host": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
+                                    C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64, _P]),
     "mpk_pipeline_run_objects": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(C.POINTER(MPObjData)),
                                        C.c_int, C.c_uint64, C.c_uint64, C.c_int]),
     "mpk_pipeline_produce": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(C.POINTER(MPObjData)),

@@ -16,6 +16,7 @@
 #include <string.h>
 #include <stdlib.h>
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "mp_internal.cuh"
@@ -344,6 +345,7 @@ struct MPLaunch {
     int njobs;
     int total_tiles;
     size_t smem;
+    double bytes;   // algorithmic bytes: inputs read once + outputs written once
 };
 
 struct MPPlanImpl {
@@ -464,6 +466,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             L.njobs = 0;
             L.total_tiles = 0;
             L.smem = smem;
+            L.bytes = 0.0;
             for (size_t q = 0; q < ch.imgs.size(); ++q) {
                 const int img = ch.imgs[q];
                 const Seg &sg = segs[img][k];
@@ -476,6 +479,8 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 if ((long long)L.total_tiles + J.ntiles > 0x7fffffffLL) return MP_ERROR_TOO_LARGE;
                 J.tile0 = L.total_tiles;
                 L.total_tiles += J.ntiles;
+                L.bytes += 4.0 * ((double)src.height * src.width * src.channels +
+                                  (double)dst.height * dst.width * dst.channels);
                 jobs.push_back(J);
                 L.njobs++;
             }
@@ -539,6 +544,34 @@ MPStatus mpk_plan_launch(MPPlan *plan, void *stream)
 int mpk_plan_num_launches(const MPPlan *plan)
 {
     return plan ? (int)((const MPPlanImpl *)plan)->launches.size() : 0;
+}
+
+MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream)
+{
+    if (!plan) return MP_ERROR_INVALID_ARGS;
+    const MPPlanImpl *P = (const MPPlanImpl *)plan;
+    if (first < 0 || count < 0 || first + count > (int)P->launches.size()) return MP_ERROR_INVALID_ARGS;
+    for (int i = first; i < first + count; ++i) {
+        const MPLaunch &L = P->launches[i];
+        MPStatus st = mp_launch_kind(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles, L.smem,
+                                     (cudaStream_t)stream);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+MPStatus mpk_plan_launch_info(const MPPlan *plan, int i, int *kind, int *njobs, int *tiles,
+                              double *bytes)
+{
+    if (!plan) return MP_ERROR_INVALID_ARGS;
+    const MPPlanImpl *P = (const MPPlanImpl *)plan;
+    if (i < 0 || i >= (int)P->launches.size()) return MP_ERROR_INVALID_ARGS;
+    const MPLaunch &L = P->launches[i];
+    if (kind) *kind = L.kind;
+    if (njobs) *njobs = L.njobs;
+    if (tiles) *tiles = L.total_tiles;
+    if (bytes) *bytes = L.bytes;
+    return MILLIPYDE_SUCCESS;
 }
 
 MPStatus mpk_plan_destroy(MPPlan *plan)
@@ -950,4 +983,139 @@ extern "C" MPStatus mpk_pipeline_produce(const MPStage *stages, int nstages, MPO
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Host-buffer batch with copy/compute overlap.
+// ---------------------------------------------------------------------------
+#define MP_HOST_CHUNK_BYTES (192ull << 20)
+
+static cudaStream_t mp_copy_stream(int dev, int which)
+{
+    static cudaStream_t streams[64][2];
+    static std::mutex mtx;
+    std::lock_guard<std::mutex> lk(mtx);
+    if (dev < 0 || dev >= 64) return nullptr;
+    if (!streams[dev][which]) {
+        if (cudaStreamCreateWithFlags(&streams[dev][which], cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            streams[dev][which] = nullptr;
+        }
+    }
+    return streams[dev][which];
+}
+
+extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, const MPImage *in,
+                                          const MPImage *out, int n, uint64_t seed, uint64_t index0,
+                                          void *stream_v)
+{
+    if (n < 0 || nstages < 0 || (n > 0 && (!in || !out))) return MP_ERROR_INVALID_ARGS;
+    if (n == 0) return MILLIPYDE_SUCCESS;
+    int dev = 0;
+    MP_CUDA_TRY(cudaGetDevice(&dev));
+    cudaStream_t cs = stream_v ? (cudaStream_t)stream_v : (cudaStream_t)mpdev_get_stream(dev, 0);
+    cudaStream_t hs = mp_copy_stream(dev, 0), ds = mp_copy_stream(dev, 1);
+    if (!cs || !hs || !ds) return MP_ERROR_NO_DEVICE;
+
+    // device geometry and chunks of consecutive images
+    std::vector<MPImage> din(n), dout(n);
+    std::vector<size_t> in_off(n), out_off(n);
+    std::vector<std::pair<int, int>> chunks;
+    size_t max_in = 0, max_out = 0;
+    {
+        size_t cin = 0, cout = 0;
+        int first = 0;
+        for (int i = 0; i < n; ++i) {
+            din[i] = in[i];
+            din[i].pitch = mp_round16((long long)in[i].width * in[i].channels * 4);
+            MPStatus st = mpk_pipeline_shapes(stages, nstages, &in[i], &dout[i], 1, seed, index0 + (uint64_t)i);
+            if (st != MILLIPYDE_SUCCESS) return st;
+            if (dout[i].height != out[i].height || dout[i].width != out[i].width ||
+                dout[i].channels != out[i].channels ||
+                out[i].pitch < out[i].width * out[i].channels * 4 ||
+                in[i].pitch < in[i].width * in[i].channels * 4)
+                return MP_ERROR_BAD_DESCRIPTOR;
+            const size_t bi = (size_t)din[i].height * din[i].pitch;
+            const size_t bo = (size_t)dout[i].height * dout[i].pitch;
+            if (i > first && cin + bi > MP_HOST_CHUNK_BYTES) {
+                chunks.push_back({first, i - first});
+                max_in = std::max(max_in, cin);
+                max_out = std::max(max_out, cout);
+                first = i;
+                cin = cout = 0;
+            }
+            in_off[i] = cin;
+            out_off[i] = cout;
+            cin += (bi + 255) / 256 * 256;
+            cout += (bo + 255) / 256 * 256;
+        }
+        chunks.push_back({first, n - first});
+        max_in = std::max(max_in, cin);
+        max_out = std::max(max_out, cout);
+    }
+    const int nslots = chunks.size() > 1 ? 2 : 1;
+    void *ibuf[2] = {nullptr, nullptr}, *obuf[2] = {nullptr, nullptr};
+    std::vector<MPPlan *> plans(chunks.size(), nullptr);
+    cudaEvent_t ev[4][2];
+    bool ev_ok = true;
+    for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 2; ++b)
+            ev_ok &= cudaEventCreateWithFlags(&ev[a][b], cudaEventDisableTiming) == cudaSuccess;
+    enum { E_H2D = 0, E_COMP = 1, E_D2H = 2, E_ALLOC = 3 };
+    MPStatus st = ev_ok ? MILLIPYDE_SUCCESS : MP_ERROR_CUDA;
+    for (int s = 0; s < nslots && st == MILLIPYDE_SUCCESS; ++s) {
+        st = mp_malloc_async(&ibuf[s], max_in, cs);
+        if (st == MILLIPYDE_SUCCESS) st = mp_malloc_async(&obuf[s], max_out, cs);
+    }
+    // every plan is created (and its job table uploaded) before any copy is
+    // queued, so the host never waits on the compute stream inside the loop
+    for (size_t k = 0; k < chunks.size() && st == MILLIPYDE_SUCCESS; ++k) {
+        const int slot = (int)(k % nslots), f = chunks[k].first, c = chunks[k].second;
+        for (int i = f; i < f + c; ++i) {
+            din[i].data = (char *)ibuf[slot] + in_off[i];
+            dout[i].data = (char *)obuf[slot] + out_off[i];
+        }
+        st = mpk_plan_create(stages, nstages, &din[f], &dout[f], c, seed, index0 + (uint64_t)f, cs,
+                             &plans[k]);
+    }
+    if (st == MILLIPYDE_SUCCESS) {
+        st = mp_cuda_status(cudaEventRecord(ev[E_ALLOC][0], cs));
+        if (st == MILLIPYDE_SUCCESS) cudaStreamWaitEvent(hs, ev[E_ALLOC][0], 0);
+        if (st == MILLIPYDE_SUCCESS) cudaStreamWaitEvent(ds, ev[E_ALLOC][0], 0);
+    }
+    for (size_t k = 0; k < chunks.size() && st == MILLIPYDE_SUCCESS; ++k) {
+        const int slot = (int)(k % nslots), f = chunks[k].first, c = chunks[k].second;
+        if (k >= (size_t)nslots) cudaStreamWaitEvent(hs, ev[E_COMP][slot], 0);   // input slot free
+        for (int i = f; i < f + c && st == MILLIPYDE_SUCCESS; ++i)
+            if (din[i].height > 0 && din[i].width > 0)
+                st = mp_cuda_status(cudaMemcpy2DAsync(din[i].data, din[i].pitch, in[i].data, in[i].pitch,
+                                                      (size_t)in[i].width * in[i].channels * 4,
+                                                      in[i].height, cudaMemcpyHostToDevice, hs));
+        if (st != MILLIPYDE_SUCCESS) break;
+        cudaEventRecord(ev[E_H2D][slot], hs);
+        cudaStreamWaitEvent(cs, ev[E_H2D][slot], 0);
+        if (k >= (size_t)nslots) cudaStreamWaitEvent(cs, ev[E_D2H][slot], 0);   // output slot free
+        st = mpk_plan_launch(plans[k], cs);
+        if (st != MILLIPYDE_SUCCESS) break;
+        cudaEventRecord(ev[E_COMP][slot], cs);
+        cudaStreamWaitEvent(ds, ev[E_COMP][slot], 0);
+        for (int i = f; i < f + c && st == MILLIPYDE_SUCCESS; ++i)
+            if (dout[i].height > 0 && dout[i].width > 0)
+                st = mp_cuda_status(cudaMemcpy2DAsync(out[i].data, out[i].pitch, dout[i].data, dout[i].pitch,
+                                                      (size_t)dout[i].width * dout[i].channels * 4,
+                                                      dout[i].height, cudaMemcpyDeviceToHost, ds));
+        cudaEventRecord(ev[E_D2H][slot], ds);
+    }
+    cudaStreamSynchronize(hs);
+    cudaStreamSynchronize(ds);
+    cudaStreamSynchronize(cs);
+    for (MPPlan *p : plans) mpk_plan_destroy(p);
+    for (int s = 0; s < 2; ++s) {
+        mp_free_async(ibuf[s], cs);
+        mp_free_async(obuf[s], cs);
+    }
+    for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 2; ++b) cudaEventDestroy(ev[a][b]);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    return mp_check_device_error(cs);
 }

@@ -8,9 +8,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-from millipyde_gb300 import _build  # noqa: E402
+import __graft_entry__  # noqa: E402
 
-_build.build()
+__graft_entry__.build()
 
 
 def pytest_configure(config):
