@@ -1,0 +1,142 @@
+"""Differentiable image chains: torch.autograd.Function over the adjoint kernels.
+
+    y = pipeline(x, [("rotate", theta), ("gaussian", sigma),
+                     ("adjust_gamma", gamma), ("rgb2grey",)])
+    (y * W).sum().backward()      # grads for x, theta, sigma, gamma
+
+x is a float32 CUDA tensor of shape (B, H, W, C) (channels last, C in 1, 3, 4)
+or (B, C, H, W) with channels_first=True.  Each op parameter is a python
+float (same for every image) or a tensor of shape (B,) (per image; may
+require grad).  adjust_gamma takes (gamma[, gain]), colorize (r, g, b).
+
+Forward runs the fused batch path (mpk_chain_forward).  Backward
+(mpk_chain_backward) saves nothing but x and the parameters: it recomputes
+the forward intermediates image chunk by image chunk (bounded scratch) and
+runs the adjoints in reverse -- one pass for each run of pointwise ops
+(with their parameter gradients), blur(g) and two derivative-tap dot passes
+for gaussian (d sigma), the exact transpose of the bilinear gather plus
+d theta for rotate, and the inverse permutation for transpose / fliplr.
+Parameter gradients accumulate in FP64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _abi
+
+# name -> (MPOpCode, number of parameters)
+_OPS = {
+    "rgb2grey": (_abi.OP_RGB2GREY, 0), "rgb2gray": (_abi.OP_RGB2GREY, 0),
+    "transpose": (_abi.OP_TRANSPOSE, 0), "fliplr": (_abi.OP_FLIPLR, 0),
+    "gaussian": (_abi.OP_GAUSSIAN, 1), "rotate": (_abi.OP_ROTATE, 1),
+    "brightness": (_abi.OP_BRIGHTNESS, 1), "adjust_gamma": (_abi.OP_ADJUST_GAMMA, 2),
+    "colorize": (_abi.OP_COLORIZE, 3),
+}
+_DEFAULTS = {"adjust_gamma": (None, 1.0)}
+
+_L = None
+
+
+def _lib():
+    global _L
+    if _L is None:
+        L = _abi.lib()
+        L.mpk_chain_shape.restype = C.c_int
+        L.mpk_chain_shape.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.mpk_chain_forward.restype = C.c_int
+        L.mpk_chain_forward.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.mpk_chain_backward.restype = C.c_int
+        L.mpk_chain_backward.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_void_p]
+        _L = L
+    return _L
+
+
+def _opcodes(names):
+    arr = (C.c_int * max(1, len(names)))()
+    for i, n in enumerate(names):
+        arr[i] = _OPS[n][0]
+    return arr
+
+
+class _ChainFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, names, slots, *ptensors):
+        B, H, W, Cc = x.shape
+        nops = len(names)
+        # host table of explicit per-image parameters [B][nops][3]
+        P = torch.zeros((B, max(1, nops), 3), dtype=torch.float64)
+        for t, (k, j) in zip(ptensors, slots):
+            P[:, k, j] = t.detach().to("cpu", torch.float64).reshape(-1).expand(B)
+        ops = _opcodes(names)
+        L = _lib()
+        ho, wo, co = C.c_int(), C.c_int(), C.c_int()
+        _abi.check(L.mpk_chain_shape(ops, nops, H, W, Cc, C.byref(ho), C.byref(wo), C.byref(co)))
+        y = torch.empty((B, ho.value, wo.value, co.value), device=x.device, dtype=torch.float32)
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        _abi.check(L.mpk_chain_forward(ops, nops, P.data_ptr(), x.data_ptr(), y.data_ptr(),
+                                       B, H, W, Cc, stream))
+        ctx.save_for_backward(x)
+        ctx.P, ctx.names, ctx.slots, ctx.nparams = P, names, slots, len(ptensors)
+        ctx.pshapes = [(t.shape, t.dtype, t.device) for t in ptensors]
+        return y
+
+    @staticmethod
+    def backward(ctx, gy):
+        (x,) = ctx.saved_tensors
+        B, H, W, Cc = x.shape
+        gy = gy.contiguous()
+        dx = torch.empty_like(x)
+        nops = len(ctx.names)
+        dP = torch.zeros((B, max(1, nops), 3), dtype=torch.float64, device=x.device)
+        L = _lib()
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        _abi.check(L.mpk_chain_backward(_opcodes(ctx.names), nops, ctx.P.data_ptr(), x.data_ptr(),
+                                        gy.data_ptr(), dx.data_ptr(), dP.data_ptr(), B, H, W, Cc, stream))
+        grads = []
+        for (k, j), (shape, dtype, dev) in zip(ctx.slots, ctx.pshapes):
+            g = dP[:, k, j]
+            g = g.sum().reshape(shape) if len(shape) == 0 or shape.numel() == 1 and B != 1 else g.reshape(shape)
+            grads.append(g.to(device=dev, dtype=dtype))
+        return (dx, None, None) + tuple(grads)
+
+
+def pipeline(x: torch.Tensor, ops, channels_first: bool = False) -> torch.Tensor:
+    """Apply a differentiable chain of image ops to a batch (see module doc).
+
+    Returns (B, Ho, Wo, Co) float32 (channels last; (B, Co, Ho, Wo) when
+    channels_first); a single output channel is squeezed: (B, Ho, Wo)."""
+    if not x.is_cuda or x.dtype != torch.float32 or x.dim() != 4:
+        raise TypeError("pipeline expects a 4-D float32 CUDA tensor")
+    if channels_first:
+        x = x.permute(0, 2, 3, 1)
+    x = x.contiguous()
+    B = x.shape[0]
+    names, slots, ptensors = [], [], []
+    for k, spec in enumerate(ops):
+        name, args = spec[0], list(spec[1:])
+        if name not in _OPS:
+            raise ValueError("unknown op %r" % name)
+        nparam = _OPS[name][1]
+        dflt = _DEFAULTS.get(name, ())
+        while len(args) < nparam and len(dflt) > len(args) and dflt[len(args)] is not None:
+            args.append(dflt[len(args)])
+        if len(args) != nparam:
+            raise ValueError("%s takes %d parameter(s)" % (name, nparam))
+        names.append(name)
+        for j, a in enumerate(args):
+            t = a if torch.is_tensor(a) else torch.tensor(float(a), dtype=torch.float64)
+            if t.numel() not in (1, B):
+                raise ValueError("parameter %d of %s must be a scalar or have %d entries" % (j, name, B))
+            slots.append((k, j))
+            ptensors.append(t)
+    y = _ChainFn.apply(x, tuple(names), tuple(slots), *ptensors)
+    if channels_first:
+        y = y.permute(0, 3, 1, 2)
+        return y[:, 0] if y.shape[1] == 1 else y
+    return y[..., 0] if y.shape[-1] == 1 else y

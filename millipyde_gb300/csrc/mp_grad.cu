@@ -1,0 +1,309 @@
+// mp_grad.cu -- adjoint kernels of the differentiable path.
+//
+//   POINT_ADJ   one pass over a run of pointwise ops (rgb2grey, brightness,
+//               adjust_gamma, colorize): recomputes the forward values of the
+//               run in registers from its input x, back-propagates the
+//               output gradient g through the run in reverse and accumulates
+//               the parameter gradients (d delta, d gamma, d gain, d mult).
+//   ROTATE_ADJ  dx = R^T g, the exact transpose of the forward bilinear
+//               gather: for each source pixel q the kernel visits the (at most
+//               4x4) output pixels p whose forward sample used q, recomputes
+//               their fixed-point sample position exactly as the forward does
+//               and applies the forward's own weight.  No atomics, so dx is
+//               deterministic.  The same tile also accumulates
+//               d theta = sum_p g(p) . d/dtheta bilinear(x, s(p)).
+// The gaussian's adjoint needs no kernel of its own: the zero-padded
+// gaussian is self-adjoint (dx = blur(g), a forward GAUSS job), and
+// d sigma = <g, (W'(x)W + W(x)W') x> is two GAUSS jobs in dot mode with
+// derivative taps (mp_kernels.cu).
+//
+// Conventions at the kinks (matching the FP64 oracle and the torch-composed
+// reference of the tests): a clamp passes gradient only strictly inside
+// (0, 1); d/dx x^gamma and d/dgamma are 0 at x = 0.
+#include "mp_internal.cuh"
+
+#define MP_THREADS 256
+#define MP_DEG2RAD_F 0.01745329252f
+
+__device__ __forceinline__ int mp_find_job_adj(const MPJob *__restrict__ jobs, int njobs, int tile)
+{
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (jobs[mid].tile0 <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ float mp_block_sum(float v, float *red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    float t = 0.f;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    return t;   // valid in thread 0
+}
+
+// One pointwise op forward (same arithmetic as mp_pw_apply).
+__device__ __forceinline__ int mp_pw_one(const PwOp &o, float v[4], int c)
+{
+    PwList L;
+    L.n = 1;
+    L.op[0] = o;
+    return mp_pw_apply(L, v, c);
+}
+
+// Back-propagates g (channels of the op's output) through op `o` whose input
+// was v (c channels).  Writes the input gradient to gi, adds parameter
+// gradients to pa[0..2].
+__device__ __forceinline__ void mp_pw_back(const PwOp &o, const float v[4], int c, const float g[4],
+                                           float gi[4], float pa[3])
+{
+    const int cc = (c == 4) ? 3 : c;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) gi[k] = g[k];
+    switch (o.op) {
+    case MP_OP_RGB2GREY: {
+        if (c < 3) break;
+        const float s = 0.2125f * v[0] + 0.7154f * v[1] + 0.0721f * v[2];
+        const float gg = (s < 1.0f) ? g[0] : 0.0f;
+        gi[0] = 0.2125f * gg;
+        gi[1] = 0.7154f * gg;
+        gi[2] = 0.0721f * gg;
+        gi[3] = 0.0f;
+        break;
+    }
+    case MP_OP_BRIGHTNESS:
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (k < cc) {
+                const float t = v[k] + o.p0;
+                const float m = (t > 0.0f && t < 1.0f) ? g[k] : 0.0f;
+                gi[k] = m;
+                pa[0] += m;
+            }
+        }
+        break;
+    case MP_OP_ADJUST_GAMMA:
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (k < cc) {
+                const float x = v[k];
+                float d = 0.0f;
+                if (x > 0.0f) {
+                    const float pw = powf(x, o.p0);
+                    const float t = o.p1 * pw;
+                    if (t > 0.0f && t < 1.0f) {
+                        d = g[k] * o.p0 * t / x;
+                        pa[0] += g[k] * t * logf(x);
+                        pa[1] += g[k] * pw;
+                    }
+                }
+                gi[k] = d;
+            }
+        }
+        break;
+    case MP_OP_COLORIZE:
+        if (c < 3) break;
+        {
+            const float m[3] = {o.p0, o.p1, o.p2};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const bool in = v[k] * m[k] < 1.0f;
+                gi[k] = in ? g[k] * m[k] : 0.0f;
+                pa[k] += in ? g[k] * v[k] : 0.0f;
+            }
+        }
+        break;
+    default:
+        break;
+    }
+}
+
+__device__ void mp_point_adj_tile(const MPJob &J, int t, float *red)
+{
+    const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
+    const int x = tx * 256 + threadIdx.x;
+    const int n = J.pro.n;
+    float pacc[MP_MAX_PW][3];
+#pragma unroll
+    for (int k = 0; k < MP_MAX_PW; ++k) pacc[k][0] = pacc[k][1] = pacc[k][2] = 0.f;
+    if (x < J.w) {
+        for (int i = 0; i < 4; ++i) {
+            const int y = ty * 4 + i;
+            if (y >= J.h) break;
+            float v[MP_MAX_PW + 1][4];
+            int cs[MP_MAX_PW + 1];
+            const float *p = J.src + (size_t)y * J.src_pitch + (size_t)x * J.cin;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) v[0][c] = (c < J.cin) ? __ldg(p + c) : 0.f;
+            cs[0] = J.cin;
+#pragma unroll
+            for (int k = 0; k < MP_MAX_PW; ++k) {
+                if (k < n) {
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) v[k + 1][c] = v[k][c];
+                    cs[k + 1] = mp_pw_one(J.pro.op[k], v[k + 1], cs[k]);
+                }
+            }
+            float g[4];
+            const int cout = cs[n];
+            const float *gp = J.aux + (size_t)y * J.aux_pitch + (size_t)x * cout;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) g[c] = (c < cout) ? __ldg(gp + c) : 0.f;
+#pragma unroll
+            for (int k = MP_MAX_PW - 1; k >= 0; --k) {
+                if (k < n) {
+                    float gi[4];
+                    mp_pw_back(J.pro.op[k], v[k], cs[k], g, gi, pacc[k]);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) g[c] = gi[c];
+                }
+            }
+            float *d = J.dst + (size_t)y * J.dst_pitch + (size_t)x * J.cin;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (c < J.cin) d[c] = g[c];
+        }
+    }
+    if (!J.acc) return;
+    for (int k = 0; k < n; ++k) {
+        const int np = (J.pro.op[k].op == MP_OP_BRIGHTNESS) ? 1
+                     : (J.pro.op[k].op == MP_OP_ADJUST_GAMMA) ? 2
+                     : (J.pro.op[k].op == MP_OP_COLORIZE) ? 3 : 0;
+        for (int j = 0; j < np; ++j) {
+            float val = 0.f;
+#pragma unroll
+            for (int kk = 0; kk < MP_MAX_PW; ++kk)
+#pragma unroll
+                for (int jj = 0; jj < 3; ++jj)
+                    if (kk == k && jj == j) val = pacc[kk][jj];
+            const float tot = mp_block_sum(val, red);
+            if (threadIdx.x == 0) atomicAdd(J.acc + J.pw_slot[k] * 3 + j, (double)tot);
+        }
+    }
+}
+
+// Forward sample position of output pixel (x, y) in MP_FIX_FRAC fixed point,
+// bit-identical to the forward ROTATE kernel.
+__device__ __forceinline__ void mp_rot_src(const MPJob &J, int x, int y, long long &sx, long long &sy)
+{
+    const long long W = J.w, H = J.h;
+    const long long X2 = 2LL * x - W, Y2 = 2LL * y - H;
+    sx = J.cosq * X2 - J.sinq * Y2 + (W << (MP_FIX_FRAC - 1));
+    sy = J.sinq * X2 + J.cosq * Y2 + (H << (MP_FIX_FRAC - 1));
+}
+
+__device__ __forceinline__ float mp_frac24(long long s)
+{
+    return (float)((int)((s >> (MP_FIX_FRAC - 24)) & 0xFFFFFF)) * 5.9604644775390625e-8f;
+}
+
+__device__ void mp_rotate_adj_tile(const MPJob &J, int t, float *red)
+{
+    const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    const int C = J.cin;
+    const float hw = 0.5f * (float)J.w, hh = 0.5f * (float)J.h;
+    float dth = 0.f;
+    for (int i = 0; i < 4; ++i) {
+        const int qx = tx * 32 + lx, qy = ty * 32 + ly + 8 * i;
+        if (qx >= J.w || qy >= J.h) continue;
+        // ---- dx(q): transpose of the forward gather
+        const float dxq = (float)qx - hw, dyq = (float)qy - hh;
+        const float pxf = J.cth * dxq + J.sth * dyq + hw;     // R(-theta)(q - c) + c
+        const float pyf = -J.sth * dxq + J.cth * dyq + hh;
+        const int px0 = (int)floorf(pxf) - 1, py0 = (int)floorf(pyf) - 1;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int py = py0; py < py0 + 4; ++py) {
+            if (py < 0 || py >= J.h) continue;
+            for (int px = px0; px < px0 + 4; ++px) {
+                if (px < 0 || px >= J.w) continue;
+                long long sx, sy;
+                mp_rot_src(J, px, py, sx, sy);
+                const int ix = (int)(sx >> MP_FIX_FRAC), iy = (int)(sy >> MP_FIX_FRAC);
+                const int ex = qx - ix, ey = qy - iy;
+                if ((unsigned)ex > 1u || (unsigned)ey > 1u) continue;
+                const float fx = mp_frac24(sx), fy = mp_frac24(sy);
+                const float wx = ex ? fx : 1.0f - fx;
+                const float wy = ey ? fy : 1.0f - fy;
+                const float w = wy * wx;
+                const float *gp = J.aux + (size_t)py * J.aux_pitch + (size_t)px * C;
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    if (c < C) acc[c] = fmaf(w, __ldg(gp + c), acc[c]);
+            }
+        }
+        float *d = J.dst + (size_t)qy * J.dst_pitch + (size_t)qx * C;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            if (c < C) d[c] = acc[c];
+        // ---- d theta contribution of output pixel p = q
+        if (J.acc) {
+            long long sx, sy;
+            mp_rot_src(J, qx, qy, sx, sy);
+            const int ix = (int)(sx >> MP_FIX_FRAC), iy = (int)(sy >> MP_FIX_FRAC);
+            const float fx = mp_frac24(sx), fy = mp_frac24(sy);
+            const float gx = 1.f - fx, gy = 1.f - fy;
+            const float dsx = (-J.sth * dxq - J.cth * dyq) * MP_DEG2RAD_F;
+            const float dsy = (J.cth * dxq - J.sth * dyq) * MP_DEG2RAD_F;
+            const float *gp = J.aux + (size_t)qy * J.aux_pitch + (size_t)qx * C;
+            for (int c = 0; c < C; ++c) {
+                float a = 0.f, b = 0.f, cc = 0.f, dd = 0.f;
+                const bool x0 = ix >= 0 && ix < J.w, x1 = ix + 1 >= 0 && ix + 1 < J.w;
+                const bool y0 = iy >= 0 && iy < J.h, y1 = iy + 1 >= 0 && iy + 1 < J.h;
+                const float *s0 = J.src + (size_t)iy * J.src_pitch + c;
+                const float *s1 = s0 + J.src_pitch;
+                if (y0 && x0) a = __ldg(s0 + (size_t)ix * C);
+                if (y0 && x1) b = __ldg(s0 + (size_t)(ix + 1) * C);
+                if (y1 && x0) cc = __ldg(s1 + (size_t)ix * C);
+                if (y1 && x1) dd = __ldg(s1 + (size_t)(ix + 1) * C);
+                const float dvx = gy * (b - a) + fy * (dd - cc);
+                const float dvy = gx * (cc - a) + fx * (dd - b);
+                dth = fmaf(__ldg(gp + c), dvx * dsx + dvy * dsy, dth);
+            }
+        }
+    }
+    if (J.acc) {
+        const float tot = mp_block_sum(dth, red);
+        if (threadIdx.x == 0) atomicAdd(J.acc, (double)tot);
+    }
+}
+
+__global__ void __launch_bounds__(MP_THREADS) mp_point_adjoint_batch(const MPJob *__restrict__ jobs,
+                                                                     int njobs, int *err)
+{
+    __shared__ float red[32];
+    const int t = blockIdx.x;
+    const MPJob &J = jobs[mp_find_job_adj(jobs, njobs, t)];
+    const int lt = t - J.tile0;
+    if (lt >= J.ntiles) return;
+    mp_point_adj_tile(J, lt, red);
+}
+
+__global__ void __launch_bounds__(MP_THREADS) mp_rotate_adjoint_batch(const MPJob *__restrict__ jobs,
+                                                                      int njobs, int *err)
+{
+    __shared__ float red[32];
+    const int t = blockIdx.x;
+    const MPJob &J = jobs[mp_find_job_adj(jobs, njobs, t)];
+    const int lt = t - J.tile0;
+    if (lt >= J.ntiles) return;
+    mp_rotate_adj_tile(J, lt, red);
+}
+
+MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, int njobs, int total_tiles, int *err,
+                           cudaStream_t s)
+{
+    if (total_tiles <= 0 || njobs <= 0) return MILLIPYDE_SUCCESS;
+    const void *fn = kind == MPK_ROTATE_ADJ ? (const void *)mp_rotate_adjoint_batch
+                                            : (const void *)mp_point_adjoint_batch;
+    void *args[] = {(void *)&jobs_dev, (void *)&njobs, (void *)&err};
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(total_tiles), dim3(MP_THREADS), args, 0, s));
+}

@@ -56,7 +56,16 @@ struct MPJob {
     int ntiles;                // tiles of this image
     int use_tma;               // GAUSS: source rows 16-byte aligned -> TMA path
     PwList pro, epi;
-    float wts[MP_MAX_TAPS];    // GAUSS: normalised taps w[0..2r]
+    float wts[MP_MAX_TAPS];    // GAUSS: normalised taps w[0..2r] (vertical pass)
+    // ---- adjoint / reduction modes (zero for plain forward jobs)
+    int hsep;                  // GAUSS: horizontal pass uses wts_h instead of wts
+    int dot;                   // GAUSS: accumulate sum(out * aux) into acc[0], write nothing
+    const float *aux;          // dot source (GAUSS) / output-space gradient (adjoints)
+    int aux_pitch;             // in floats
+    double *acc;               // per-image accumulators (parameter gradients)
+    int pw_slot[MP_MAX_PW];    // POINT adjoint: acc slot (x3) of each pointwise op
+    float cth, sth;            // ROTATE adjoint: cos/sin of the angle
+    float wts_h[MP_MAX_TAPS];  // GAUSS: horizontal taps when hsep
 };
 
 // ---------------------------------------------------------------------------
@@ -208,9 +217,16 @@ void mp_free_async(void *p, cudaStream_t s);
 // Kernel launchers (mp_kernels.cu).  `jobs` is a device table of njobs jobs
 // sorted by tile0; `total_tiles` the sum of their ntiles.
 MPStatus mp_launch_kind(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
-                        size_t smem_bytes, cudaStream_t s);
+                        size_t smem_bytes, int *err, cudaStream_t s);
+// Sets the dynamic shared-memory limit a (kind, smem) launch needs; call
+// outside stream capture.
+MPStatus mp_prepare_kind(int kind, size_t smem_bytes);
 // Single-job launch with the job passed by value (no device table).
 MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem_bytes, cudaStream_t s);
+// Adjoint kernels (mp_grad.cu), one job per image, tiles as the forward kinds.
+enum { MPK_POINT_ADJ = 10, MPK_ROTATE_ADJ = 11 };
+MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
+                           int *err, cudaStream_t s);
 // In-place channel-agnostic pointwise list over n contiguous floats.
 MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s);
 // Dynamic shared memory a GAUSS launch needs for the given geometry.

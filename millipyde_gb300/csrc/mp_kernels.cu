@@ -10,6 +10,10 @@
 // Every kernel reads its work from an MPJob (one per image).  A launch covers
 // a ragged batch: blockIdx.x is a global tile index, mapped to its image by a
 // binary search over the jobs' tile offsets.
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "mp_internal.cuh"
 
 #define MP_THREADS 256
@@ -31,7 +35,8 @@ __device__ __forceinline__ int mp_find_job(const MPJob *__restrict__ jobs, int n
 // ---------------------------------------------------------------------------
 // GAUSS shared-memory layout (host and device agree on it).
 //   [0,16)        mbarrier
-//   [16, 16+4*T)  taps (T = MP_MAX_TAPS, rounded to 16 floats)
+//   [16, ...)     vertical taps, horizontal taps (MP_MAX_TAPS rounded to 16
+//                 floats each), 32 floats of reduction scratch
 //   A (128-B aligned): TMA tile S, later vT (prologue) or obuf (no prologue)
 //   B (128-B aligned): vT (no prologue) or G then obuf (prologue)
 // All sizes in floats unless noted.
@@ -66,7 +71,8 @@ __host__ __device__ __forceinline__ GaussGeom mp_gauss_geom(int tw, int th, int 
         A = S > ob ? S : ob;
         B = vT;
     }
-    const int head = mp_round_up(16 + 4 * mp_round_up(MP_MAX_TAPS, 16), 128);
+    // mbarrier, vertical taps, horizontal taps, 32-float reduction scratch
+    const int head = mp_round_up(16 + 8 * mp_round_up(MP_MAX_TAPS, 16) + 4 * 32, 128);
     g.offA = head;
     g.offB = g.offA + mp_round_up(A * 4, 128);
     g.total = g.offB + mp_round_up(B * 4, 128);
@@ -76,6 +82,23 @@ __host__ __device__ __forceinline__ GaussGeom mp_gauss_geom(int tw, int th, int 
 size_t mp_gauss_smem_bytes(int tw, int th, int radius, int cin, int cmid, int has_pro)
 {
     return (size_t)mp_gauss_geom(tw, th, radius, cin, cmid, has_pro).total + 128;  // +128: alignment slack
+}
+
+// Block-wide sum of one float per thread, added (FP64) to *acc by thread 0.
+// `red` is 32 floats of shared memory.  All threads of the block must call.
+__device__ __forceinline__ void mp_block_add(float v, float *red, double *acc)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        atomicAdd(acc, (double)t);
+    }
 }
 
 // 1-D correlation along the row index of a [rows][stride] float array,
@@ -130,6 +153,8 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
         smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
     uint64_t *bar = reinterpret_cast<uint64_t *>(base);
     float *wsm = reinterpret_cast<float *>(base + 16);
+    float *wsm_h = wsm + mp_round_up(MP_MAX_TAPS, 16);
+    float *red = wsm_h + mp_round_up(MP_MAX_TAPS, 16);
     float *A = reinterpret_cast<float *>(base + g.offA);
     float *B = reinterpret_cast<float *>(base + g.offB);
     float *S = A;
@@ -140,7 +165,10 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
     const int nbx = (delta + (tw + 2 * r) * cin + 63) / 64;
     const int ntaps = 2 * r + 1;
 
-    for (int i = threadIdx.x; i < ntaps; i += blockDim.x) wsm[i] = J.wts[i];
+    for (int i = threadIdx.x; i < ntaps; i += blockDim.x) {
+        wsm[i] = J.wts[i];
+        wsm_h[i] = J.hsep ? J.wts_h[i] : J.wts[i];
+    }
 
     if (J.use_tma) {
         if (threadIdx.x == 0) {
@@ -258,7 +286,7 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
         float4 acc[8];
 #pragma unroll
         for (int o = 0; o < 8; ++o) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-        mp_conv8(vT + ((8 * b) * cmid + c) * g.RBp + 4 * a, cmid * g.RBp, ntaps, wsm, acc);
+        mp_conv8(vT + ((8 * b) * cmid + c) * g.RBp + 4 * a, cmid * g.RBp, ntaps, wsm_h, acc);
 #pragma unroll
         for (int o = 0; o < 8; ++o) {
             float *dst = obuf + (4 * a) * g.OBW + (8 * b + o) * cmid + c;
@@ -270,6 +298,19 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
     }
     __syncthreads();
 
+    // ---- 5a. dot mode: sum(out * aux) over the tile into acc[0]
+    if (J.dot) {
+        float part = 0.f;
+        for (int i = threadIdx.x; i < th * tw; i += blockDim.x) {
+            const int tt = i / tw, xx = i - tt * tw;
+            const int gyy = y0 + tt, gxx = x0 + xx;
+            if (gyy >= J.h || gxx >= J.w) continue;
+            const float *d = J.aux + (size_t)gyy * J.aux_pitch + (size_t)gxx * cmid;
+            for (int c = 0; c < cmid; ++c) part = fmaf(obuf[tt * g.OBW + xx * cmid + c], d[c], part);
+        }
+        mp_block_add(part, red, J.acc);
+        return;
+    }
     // ---- 5. copy-out with epilogue and output map
     for (int i = threadIdx.x; i < th * tw; i += blockDim.x) {
         const int tt = i / tw, xx = i - tt * tw;
@@ -432,8 +473,7 @@ __device__ __forceinline__ void mp_run_tile(const MPJob &J, int lt, bool map_in_
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(MP_THREADS) mp_k_batch(const MPJob *__restrict__ jobs, int njobs,
-                                                         int *err)
+__device__ __forceinline__ void mp_batch_body(const MPJob *__restrict__ jobs, int njobs, int *err)
 {
     const int t = blockIdx.x;
     const int j = mp_find_job(jobs, njobs, t);
@@ -443,11 +483,22 @@ __global__ void __launch_bounds__(MP_THREADS) mp_k_batch(const MPJob *__restrict
     mp_run_tile<KIND>(J, lt, true, err);
 }
 
-template <int KIND>
-__global__ void __launch_bounds__(MP_THREADS) mp_k_single(const __grid_constant__ MPJob job, int *err)
-{
-    mp_run_tile<KIND>(job, blockIdx.x, false, err);
-}
+// One named kernel per kind and launch form, so profiles name what ran.
+#define MP_DEFINE_KERNELS(NAME, KIND)                                                        \
+    __global__ void __launch_bounds__(MP_THREADS)                                            \
+        NAME##_batch(const MPJob *__restrict__ jobs, int njobs, int *err)                    \
+    {                                                                                        \
+        mp_batch_body<KIND>(jobs, njobs, err);                                               \
+    }                                                                                        \
+    __global__ void __launch_bounds__(MP_THREADS) NAME##_single(const __grid_constant__ MPJob job, \
+                                                                int *err)                    \
+    {                                                                                        \
+        mp_run_tile<KIND>(job, blockIdx.x, false, err);                                      \
+    }
+MP_DEFINE_KERNELS(mp_gauss, MPK_GAUSS)
+MP_DEFINE_KERNELS(mp_rotate, MPK_ROTATE)
+MP_DEFINE_KERNELS(mp_transpose, MPK_TRANSPOSE)
+MP_DEFINE_KERNELS(mp_point, MPK_POINT)
 
 // In-place channel-agnostic pointwise list (brightness, gamma) over a flat
 // float buffer: float4 body plus scalar tail.
@@ -478,13 +529,26 @@ __global__ void __launch_bounds__(MP_THREADS) mp_k_flat(float *__restrict__ data
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum the first time a launch needs more than the 48 KB default.  The
+// limit only ever grows, so launches prepared earlier stay valid.
 static MPStatus mp_prepare_smem(const void *fn, size_t smem)
 {
-    if (smem > 48 * 1024) {
-        cudaError_t e =
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return mp_cuda_status(e);
-    }
+    if (smem <= 48 * 1024) return MILLIPYDE_SUCCESS;
+    static std::mutex mtx;
+    static std::vector<std::pair<const void *, int>> done;   // (kernel, device)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mtx);
+    for (auto &d : done)
+        if (d.first == fn && d.second == dev) return MILLIPYDE_SUCCESS;
+    int optin = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return mp_cuda_status(e);
+    if ((size_t)optin < smem) return MP_ERROR_TOO_LARGE;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess) return mp_cuda_status(e);
+    done.push_back({fn, dev});
     return MILLIPYDE_SUCCESS;
 }
 
@@ -495,20 +559,28 @@ static int mp_current_device()
     return d;
 }
 
+static const void *mp_batch_fn(int kind)
+{
+    switch (kind) {
+    case MPK_GAUSS: return (const void *)mp_gauss_batch;
+    case MPK_ROTATE: return (const void *)mp_rotate_batch;
+    case MPK_TRANSPOSE: return (const void *)mp_transpose_batch;
+    default: return (const void *)mp_point_batch;
+    }
+}
+
+MPStatus mp_prepare_kind(int kind, size_t smem)
+{
+    return mp_prepare_smem(mp_batch_fn(kind), smem);
+}
+
+// Kernel launch only (no allocation, no attribute change), so it may be
+// captured into a CUDA graph; mp_prepare_kind must have run for (kind, smem).
 MPStatus mp_launch_kind(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
-                        size_t smem, cudaStream_t s)
+                        size_t smem, int *err, cudaStream_t s)
 {
     if (total_tiles <= 0 || njobs <= 0) return MILLIPYDE_SUCCESS;
-    int *err = mp_device_error_word(mp_current_device());
-    const void *fn;
-    switch (kind) {
-    case MPK_GAUSS: fn = (const void *)mp_k_batch<MPK_GAUSS>; break;
-    case MPK_ROTATE: fn = (const void *)mp_k_batch<MPK_ROTATE>; break;
-    case MPK_TRANSPOSE: fn = (const void *)mp_k_batch<MPK_TRANSPOSE>; break;
-    default: fn = (const void *)mp_k_batch<MPK_POINT>; break;
-    }
-    MPStatus st = mp_prepare_smem(fn, smem);
-    if (st != MILLIPYDE_SUCCESS) return st;
+    const void *fn = mp_batch_fn(kind);
     void *args[] = {(void *)&jobs_dev, (void *)&njobs, (void *)&err};
     return mp_cuda_status(
         cudaLaunchKernel(fn, dim3(total_tiles), dim3(MP_THREADS), args, smem, s));
@@ -520,10 +592,10 @@ MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem, cudaStream_t 
     int *err = mp_device_error_word(mp_current_device());
     const void *fn;
     switch (kind) {
-    case MPK_GAUSS: fn = (const void *)mp_k_single<MPK_GAUSS>; break;
-    case MPK_ROTATE: fn = (const void *)mp_k_single<MPK_ROTATE>; break;
-    case MPK_TRANSPOSE: fn = (const void *)mp_k_single<MPK_TRANSPOSE>; break;
-    default: fn = (const void *)mp_k_single<MPK_POINT>; break;
+    case MPK_GAUSS: fn = (const void *)mp_gauss_single; break;
+    case MPK_ROTATE: fn = (const void *)mp_rotate_single; break;
+    case MPK_TRANSPOSE: fn = (const void *)mp_transpose_single; break;
+    default: fn = (const void *)mp_point_single; break;
     }
     MPStatus st = mp_prepare_smem(fn, smem);
     if (st != MILLIPYDE_SUCCESS) return st;

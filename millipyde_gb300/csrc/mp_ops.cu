@@ -352,16 +352,22 @@ struct MPPlanImpl {
     std::vector<MPLaunch> launches;
     MPJob *jobs_dev = nullptr;
     void *scratch = nullptr;
+    int *err = nullptr;        // device error word the kernels report into
     int device = 0;
     cudaStream_t stream = nullptr;
 };
 
 static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage *in,
                               const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
-                              cudaStream_t s, MPPlanImpl *P)
+                              cudaStream_t s, MPPlanImpl *P,
+                              const std::vector<std::vector<ROp>> *explicit_ops = nullptr)
 {
-    if (nimgs < 0 || nstages < 0 || (nimgs > 0 && (!in || !out)) || (nstages > 0 && !stages))
+    if (nimgs < 0 || nstages < 0 || (nimgs > 0 && (!in || !out)) ||
+        (nstages > 0 && !stages && !explicit_ops))
         return MP_ERROR_BAD_DESCRIPTOR;
+    // device set-up (error word, pool) happens here, never during a capture
+    P->err = mp_device_error_word(P->device);
+    if (!P->err) return MP_ERROR_NO_DEVICE;
     // 1. resolve + segment every image
     std::vector<std::vector<Seg>> segs(nimgs);
     std::vector<ROp> ops;
@@ -371,8 +377,16 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             return MP_ERROR_BAD_DESCRIPTOR;
         if ((long long)in[i].width * in[i].channels * 4 > in[i].pitch && in[i].height > 0)
             return MP_ERROR_BAD_DESCRIPTOR;
-        MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, nullptr);
-        if (st != MILLIPYDE_SUCCESS) return st;
+        if (explicit_ops) {
+            ops = (*explicit_ops)[i];
+            for (const ROp &r : ops) {
+                MPStatus c = mp_check_op(r.op, r.p);
+                if (c != MILLIPYDE_SUCCESS) return c;
+            }
+        } else {
+            MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, nullptr);
+            if (st != MILLIPYDE_SUCCESS) return st;
+        }
         mp_segment(ops, in[i].channels, in[i].height, in[i].width, segs[i]);
         const Seg &last = segs[i].back();
         if (!out[i].data && (long long)last.hout * last.wout > 0) return MP_ERROR_NULL_DATA;
@@ -484,7 +498,11 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 jobs.push_back(J);
                 L.njobs++;
             }
-            if (L.njobs > 0) P->launches.push_back(L);
+            if (L.njobs > 0) {
+                st = mp_prepare_kind(L.kind, L.smem);
+                if (st != MILLIPYDE_SUCCESS) return st;
+                P->launches.push_back(L);
+            }
         }
     }
     if (!jobs.empty()) {
@@ -499,8 +517,11 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
 static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
 {
     for (const MPLaunch &L : P->launches) {
-        MPStatus st = mp_launch_kind(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles,
-                                     L.smem, s);
+        MPStatus st = L.kind >= MPK_POINT_ADJ
+                          ? mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles,
+                                              P->err, s)
+                          : mp_launch_kind(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles,
+                                           L.smem, P->err, s);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -554,7 +575,7 @@ MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream)
     for (int i = first; i < first + count; ++i) {
         const MPLaunch &L = P->launches[i];
         MPStatus st = mp_launch_kind(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles, L.smem,
-                                     (cudaStream_t)stream);
+                                     P->err, (cudaStream_t)stream);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -1118,4 +1139,343 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
         for (int b = 0; b < 2; ++b) cudaEventDestroy(ev[a][b]);
     if (st != MILLIPYDE_SUCCESS) return st;
     return mp_check_device_error(cs);
+}
+
+// ---------------------------------------------------------------------------
+// Differentiable chains on dense batches (the autograd path).
+//   x: B images of H x W x C float32, packed (pitch W*C*4), image b at
+//   x + b*H*W*C; ops[nops] op codes; params[(b*nops + k)*3 + j] explicit
+//   per-image parameters (angle / sigma / delta / gamma, gain / r, g, b).
+// ---------------------------------------------------------------------------
+struct MPShape { int h, w, c; };
+
+static MPStatus mp_chain_shapes(const int *ops, int nops, int H, int W, int C,
+                                std::vector<MPShape> &sh)
+{
+    if (nops < 0 || H < 0 || W < 0 || (C != 1 && C != 3 && C != 4)) return MP_ERROR_BAD_DESCRIPTOR;
+    sh.assign(nops + 1, MPShape{H, W, C});
+    for (int k = 0; k < nops; ++k) {
+        MPShape n = sh[k];
+        switch (ops[k]) {
+        case MP_OP_RGB2GREY: if (n.c >= 3) n.c = 1; break;
+        case MP_OP_TRANSPOSE: std::swap(n.h, n.w); break;
+        case MP_OP_GAUSSIAN: case MP_OP_FLIPLR: case MP_OP_ROTATE: case MP_OP_BRIGHTNESS:
+        case MP_OP_ADJUST_GAMMA: case MP_OP_COLORIZE: break;
+        default: return MP_ERROR_BAD_DESCRIPTOR;
+        }
+        sh[k + 1] = n;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+static MPImage mp_dense_image(const float *base, int b, const MPShape &s)
+{
+    MPImage m;
+    m.data = (void *)(base + (size_t)b * s.h * s.w * s.c);
+    m.height = s.h;
+    m.width = s.w;
+    m.channels = s.c;
+    m.pitch = s.w * s.c * 4;
+    return m;
+}
+
+static ROp mp_rop(int op, const double *p)
+{
+    ROp r;
+    r.op = op;
+    r.p[0] = p[0];
+    r.p[1] = p[1];
+    r.p[2] = p[2];
+    return r;
+}
+
+extern "C" MPStatus mpk_chain_shape(const int *ops, int nops, int H, int W, int C, int *Ho, int *Wo,
+                                    int *Co)
+{
+    std::vector<MPShape> sh;
+    MPStatus st = mp_chain_shapes(ops, nops, H, W, C, sh);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    if (Ho) *Ho = sh.back().h;
+    if (Wo) *Wo = sh.back().w;
+    if (Co) *Co = sh.back().c;
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_chain_forward(const int *ops, int nops, const double *params, const float *x,
+                                      float *y, int B, int H, int W, int C, void *stream)
+{
+    if (B < 0 || (B > 0 && (!x || !y || (nops > 0 && (!ops || !params))))) return MP_ERROR_INVALID_ARGS;
+    std::vector<MPShape> sh;
+    MPStatus st = mp_chain_shapes(ops, nops, H, W, C, sh);
+    if (st != MILLIPYDE_SUCCESS || B == 0) return st;
+    std::vector<MPImage> in(B), out(B);
+    std::vector<std::vector<ROp>> per(B);
+    for (int b = 0; b < B; ++b) {
+        in[b] = mp_dense_image(x, b, sh[0]);
+        out[b] = mp_dense_image(y, b, sh.back());
+        for (int k = 0; k < nops; ++k) per[b].push_back(mp_rop(ops[k], params + ((size_t)b * nops + k) * 3));
+    }
+    MPPlanImpl P;
+    cudaGetDevice(&P.device);
+    P.stream = (cudaStream_t)stream;
+    st = mp_plan_build(nullptr, 0, in.data(), out.data(), B, 0, 0, P.stream, &P, &per);
+    if (st == MILLIPYDE_SUCCESS) st = mp_plan_launch(&P, P.stream);
+    mp_plan_free(&P, P.stream);
+    return st;
+}
+
+// Derivative of the normalised gaussian taps with respect to sigma:
+// w'_k = w_k (k^2 - sum_j w_j j^2) / sigma^3.
+static void mp_gauss_taps(double sigma, int r, float *w, float *dw)
+{
+    double e[MP_MAX_TAPS], sum = 0.0, m2 = 0.0;
+    for (int k = -r; k <= r; ++k) {
+        e[k + r] = exp(-(double)(k * k) / (2.0 * sigma * sigma));
+        sum += e[k + r];
+    }
+    for (int k = -r; k <= r; ++k) m2 += e[k + r] / sum * (double)(k * k);
+    for (int k = -r; k <= r; ++k) {
+        const double wk = e[k + r] / sum;
+        w[k + r] = (float)wk;
+        if (dw) dw[k + r] = (float)(wk * ((double)(k * k) - m2) / (sigma * sigma * sigma));
+    }
+}
+
+#define MP_BWD_SCRATCH_BYTES (2048ull << 20)
+
+extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *params, const float *x,
+                                       const float *dy, float *dx, double *dparams, int B, int H,
+                                       int W, int C, void *stream)
+{
+    if (B < 0 || (B > 0 && (!x || !dy || !dx || (nops > 0 && (!ops || !params)))))
+        return MP_ERROR_INVALID_ARGS;
+    std::vector<MPShape> sh;
+    MPStatus st = mp_chain_shapes(ops, nops, H, W, C, sh);
+    if (st != MILLIPYDE_SUCCESS || B == 0) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int *err = mp_device_error_word(dev);
+    if (!err) return MP_ERROR_NO_DEVICE;
+    for (int b = 0; b < B; ++b)
+        for (int k = 0; k < nops; ++k) {
+            MPStatus c = mp_check_op(ops[k], params + ((size_t)b * nops + k) * 3);
+            if (c != MILLIPYDE_SUCCESS) return c;
+        }
+    if (nops == 0) {
+        return mp_cuda_status(cudaMemcpyAsync(dx, dy, (size_t)B * H * W * C * 4,
+                                              cudaMemcpyDeviceToDevice, s));
+    }
+    // scratch per image: intermediates a_1..a_{n-1} + two gradient buffers
+    size_t inter = 0, gmax = 0;
+    std::vector<size_t> aoff(nops + 1, 0);
+    for (int k = 1; k < nops; ++k) {
+        aoff[k] = inter;
+        inter += (size_t)sh[k].h * sh[k].w * sh[k].c * 4;
+    }
+    for (int k = 0; k <= nops; ++k) gmax = std::max(gmax, (size_t)sh[k].h * sh[k].w * sh[k].c * 4);
+    const size_t per_img = inter + 2 * gmax;
+    int chunk = (int)std::max<size_t>(1, MP_BWD_SCRATCH_BYTES / std::max<size_t>(per_img, 1));
+    chunk = std::min(chunk, B);
+    void *scratch = nullptr;
+    st = mp_malloc_async(&scratch, per_img * (size_t)chunk, s);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    char *sbase = (char *)scratch;
+    for (int b0 = 0; b0 < B && st == MILLIPYDE_SUCCESS; b0 += chunk) {
+        const int nb = std::min(chunk, B - b0);
+        // per-image pointers inside the chunk's scratch
+        auto a_img = [&](int q, int k) -> MPImage {       // input of op k for image b0+q
+            if (k == 0) return mp_dense_image(x, b0 + q, sh[0]);
+            MPImage m = mp_dense_image((const float *)(sbase + (size_t)q * per_img + aoff[k]), 0, sh[k]);
+            return m;
+        };
+        auto g_img = [&](int q, int which, const MPShape &shp) -> MPImage {
+            return mp_dense_image((const float *)(sbase + (size_t)q * per_img + inter + which * gmax), 0, shp);
+        };
+        MPPlanImpl P;
+        P.device = dev;
+        P.stream = s;
+        P.err = err;
+        std::vector<MPJob> jobs;
+        auto add_launch = [&](int kind, size_t smem, std::vector<MPJob> &js) -> MPStatus {
+            MPLaunch L;
+            L.kind = kind;
+            L.job_off = jobs.size();
+            L.njobs = 0;
+            L.total_tiles = 0;
+            L.smem = smem;
+            L.bytes = 0;
+            for (MPJob &J : js) {
+                if (J.ntiles <= 0) continue;
+                J.tile0 = L.total_tiles;
+                L.total_tiles += J.ntiles;
+                jobs.push_back(J);
+                L.njobs++;
+            }
+            if (L.njobs == 0) return MILLIPYDE_SUCCESS;
+            if (kind < MPK_POINT_ADJ) {
+                MPStatus e = mp_prepare_kind(kind, smem);
+                if (e != MILLIPYDE_SUCCESS) return e;
+            }
+            P.launches.push_back(L);
+            return MILLIPYDE_SUCCESS;
+        };
+        // one-op segment for op k of image q
+        auto seg_of = [&](int q, int k) -> Seg {
+            std::vector<ROp> one(1, mp_rop(ops[k], params + ((size_t)(b0 + q) * nops + k) * 3));
+            std::vector<Seg> sg;
+            mp_segment(one, sh[k].c, sh[k].h, sh[k].w, sg);
+            return sg.back();
+        };
+        auto gauss_launch = [&](std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> &items,
+                                std::vector<MPJob> &js, size_t *smem) -> MPStatus {
+            int rmax = 1, cm = 1;
+            for (auto &it : items) {
+                rmax = std::max(rmax, (int)ceil(3.0 * it.first.core_p[0]));
+                cm = std::max(cm, it.first.cmid);
+            }
+            int tw, th;
+            mp_gauss_tiles(rmax, cm, cm, 0, &tw, &th);
+            *smem = mp_gauss_smem_bytes(tw, th, rmax, cm, cm, 0);
+            for (auto &it : items) {
+                MPJob J;
+                MPStatus e = mp_fill_job(J, it.first, it.second.first, it.second.second, tw, th);
+                if (e != MILLIPYDE_SUCCESS) return e;
+                js.push_back(J);
+            }
+            return MILLIPYDE_SUCCESS;
+        };
+        // ---- forward recompute: a_{k+1} = op_k(a_k), k = 0..n-2
+        for (int k = 0; k + 1 < nops && st == MILLIPYDE_SUCCESS; ++k) {
+            std::vector<MPJob> js;
+            size_t smem = 0;
+            const int kind = seg_of(0, k).kind;
+            if (kind == MPK_GAUSS) {
+                std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> items;
+                for (int q = 0; q < nb; ++q) items.push_back({seg_of(q, k), {a_img(q, k), a_img(q, k + 1)}});
+                st = gauss_launch(items, js, &smem);
+            } else {
+                for (int q = 0; q < nb && st == MILLIPYDE_SUCCESS; ++q) {
+                    MPJob J;
+                    st = mp_fill_job(J, seg_of(q, k), a_img(q, k), a_img(q, k + 1), 0, 0);
+                    js.push_back(J);
+                }
+            }
+            if (st == MILLIPYDE_SUCCESS) st = add_launch(kind, smem, js);
+        }
+        // ---- reverse sweep
+        int cur = -1;   // gradient buffer holding g (output of op k); -1: dy
+        int k = nops - 1;
+        while (k >= 0 && st == MILLIPYDE_SUCCESS) {
+            int j = k;
+            const bool pw = mp_is_pointwise(ops[k]);
+            if (pw)
+                while (j > 0 && mp_is_pointwise(ops[j - 1]) && k - (j - 1) < MP_MAX_PW) --j;
+            const int nxt = (j == 0) ? -2 : (cur == 0 ? 1 : 0);   // -2: write dx
+            auto gin_img = [&](int q) -> MPImage {
+                return nxt == -2 ? mp_dense_image(dx, b0 + q, sh[0]) : g_img(q, nxt, sh[j]);
+            };
+            auto gout_img = [&](int q) -> MPImage {
+                return cur == -1 ? mp_dense_image(dy, b0 + q, sh[nops]) : g_img(q, cur, sh[k + 1]);
+            };
+            std::vector<MPJob> js;
+            if (pw) {
+                for (int q = 0; q < nb; ++q) {
+                    MPJob J;
+                    Seg sg;
+                    memset(&sg, 0, sizeof(sg));
+                    sg.kind = MPK_POINT;
+                    sg.cin = sh[j].c;
+                    for (int t = j; t <= k; ++t) {
+                        ROp r = mp_rop(ops[t], params + ((size_t)(b0 + q) * nops + t) * 3);
+                        mp_pw_push(sg.pro, r);
+                    }
+                    const MPImage a = a_img(q, j), go = gout_img(q), gi = gin_img(q);
+                    st = mp_fill_job(J, sg, a, gi, 0, 0);
+                    if (st != MILLIPYDE_SUCCESS) break;
+                    J.cin = sh[j].c;
+                    J.aux = (const float *)go.data;
+                    J.aux_pitch = go.pitch / 4;
+                    J.acc = dparams ? dparams + (size_t)(b0 + q) * nops * 3 : nullptr;
+                    for (int t = j; t <= k; ++t) J.pw_slot[t - j] = t;
+                    js.push_back(J);
+                }
+                if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_POINT_ADJ, 0, js);
+            } else if (ops[k] == MP_OP_GAUSSIAN) {
+                // dx = blur(g)
+                std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> items;
+                for (int q = 0; q < nb; ++q) items.push_back({seg_of(q, k), {gout_img(q), gin_img(q)}});
+                size_t smem = 0;
+                st = gauss_launch(items, js, &smem);
+                if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_GAUSS, smem, js);
+                // d sigma = <g, (W' (x) W + W (x) W') a_k>: two dot-mode launches
+                for (int pass = 0; pass < 2 && dparams && st == MILLIPYDE_SUCCESS; ++pass) {
+                    std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> it2;
+                    for (int q = 0; q < nb; ++q) it2.push_back({seg_of(q, k), {a_img(q, k), gout_img(q)}});
+                    std::vector<MPJob> jd;
+                    st = gauss_launch(it2, jd, &smem);
+                    for (int q = 0; q < nb && st == MILLIPYDE_SUCCESS; ++q) {
+                        MPJob &J = jd[q];
+                        float w[MP_MAX_TAPS], dw[MP_MAX_TAPS];
+                        mp_gauss_taps(it2[q].first.core_p[0], J.radius, w, dw);
+                        for (int t = 0; t < 2 * J.radius + 1; ++t) {
+                            J.wts[t] = pass == 0 ? dw[t] : w[t];
+                            J.wts_h[t] = pass == 0 ? w[t] : dw[t];
+                        }
+                        J.hsep = 1;
+                        J.dot = 1;
+                        const MPImage go = gout_img(q);
+                        J.aux = (const float *)go.data;
+                        J.aux_pitch = go.pitch / 4;
+                        J.dst = nullptr;
+                        J.acc = dparams + ((size_t)(b0 + q) * nops + k) * 3;
+                    }
+                    if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_GAUSS, smem, jd);
+                }
+            } else if (ops[k] == MP_OP_ROTATE) {
+                for (int q = 0; q < nb && st == MILLIPYDE_SUCCESS; ++q) {
+                    MPJob J;
+                    const Seg sg = seg_of(q, k);
+                    const MPImage a = a_img(q, k), go = gout_img(q), gi = gin_img(q);
+                    st = mp_fill_job(J, sg, a, gi, 0, 0);
+                    const double th_r = sg.core_p[0] * MP_DEG2RAD;
+                    J.cth = (float)cos(th_r);
+                    J.sth = (float)sin(th_r);
+                    J.aux = (const float *)go.data;
+                    J.aux_pitch = go.pitch / 4;
+                    J.acc = dparams ? dparams + ((size_t)(b0 + q) * nops + k) * 3 : nullptr;
+                    js.push_back(J);
+                }
+                if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_ROTATE_ADJ, 0, js);
+            } else {
+                // transpose / fliplr: the adjoint is the same permutation of g
+                for (int q = 0; q < nb && st == MILLIPYDE_SUCCESS; ++q) {
+                    MPJob J;
+                    const Seg sg = seg_of(q, k);
+                    const MPImage go = gout_img(q), gi = gin_img(q);
+                    Seg g2 = sg;
+                    if (ops[k] == MP_OP_TRANSPOSE) {
+                        g2.hin = sh[k + 1].h;
+                        g2.win = sh[k + 1].w;
+                    }
+                    st = mp_fill_job(J, g2, go, gi, 0, 0);
+                    js.push_back(J);
+                }
+                if (st == MILLIPYDE_SUCCESS) st = add_launch(ops[k] == MP_OP_TRANSPOSE ? MPK_TRANSPOSE : MPK_POINT, 0, js);
+            }
+            cur = nxt;
+            k = j - 1;
+        }
+        if (st == MILLIPYDE_SUCCESS && !jobs.empty()) {
+            st = mp_malloc_async((void **)&P.jobs_dev, jobs.size() * sizeof(MPJob), s);
+            if (st == MILLIPYDE_SUCCESS)
+                st = mp_cuda_status(cudaMemcpyAsync(P.jobs_dev, jobs.data(), jobs.size() * sizeof(MPJob),
+                                                    cudaMemcpyHostToDevice, s));
+        }
+        if (st == MILLIPYDE_SUCCESS) st = mp_plan_launch(&P, s);
+        mp_free_async(P.jobs_dev, s);
+        P.jobs_dev = nullptr;
+    }
+    mp_free_async(scratch, s);
+    return st;
 }

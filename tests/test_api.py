@@ -119,3 +119,10 @@ def test_no_device_raises_runtime_error_not_crash():
 def test_seed_and_counter():
     assert 0.0 <= mp._millipyde._counter_uniform(1, 2, 3, 0) < 1.0
     mp.seed(3)
+
+
+def test_autograd_wrapper_validates_on_cpu():
+    torch = pytest.importorskip("torch")
+    from millipyde_gb300.autograd import pipeline
+    with pytest.raises(TypeError):
+        pipeline(torch.zeros(1, 4, 4, 3), [("rotate", 1.0)])

@@ -219,3 +219,40 @@ def test_plan_replay_and_cuda_graph(gpu, rng):
         assert maxabs(a, ref) <= TOL
     _abi.check(L.mpk_plan_destroy(plan))
     torch.cuda.synchronize()
+
+
+_FRESH_CAPTURE = r"""
+import ctypes as C, sys
+sys.path.insert(0, sys.argv[1])
+import torch
+from millipyde_gb300 import _abi
+L = _abi.lib()
+x = torch.rand(2, 64, 64 * 3, device="cuda")
+y = torch.empty(2, 64, 64, device="cuda")
+st = _abi.stages(_abi.stage("rgb2grey"), _abi.stage("gaussian", 3.0), _abi.stage("rotate", 9.0))
+ins = _abi.images([_abi.image(x[i].data_ptr(), 64, 64, 3, 768) for i in range(2)])
+outs = _abi.images([_abi.image(y[i].data_ptr(), 64, 64, 1, 256) for i in range(2)])
+s = torch.cuda.Stream()
+plan = C.c_void_p()
+_abi.check(L.mpk_plan_create(st, 3, ins, outs, 2, 0, 0, C.c_void_p(s.cuda_stream), C.byref(plan)))
+s.synchronize()
+g = torch.cuda.CUDAGraph()
+with torch.cuda.graph(g, stream=s):
+    _abi.check(L.mpk_plan_launch(plan, C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+g.replay()
+torch.cuda.synchronize()
+print("ok", float(y.sum()))
+"""
+
+
+def test_plan_capture_in_fresh_process(gpu):
+    """The first library call of a process may be a plan whose launch is
+    captured: all device set-up must happen at plan creation."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _FRESH_CAPTURE, root], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert r.stdout.startswith("ok")
