@@ -42,6 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_IMG, H, W, CH = 256, 1024, 1024, 3
+N_IMG_DEFAULT = N_IMG
 SIGMA, ANGLE, GAMMA = 3.0, 17.0, 0.8
 SEED = 20260303
 METRIC = "Mpix/s fused pipeline fwd (grey->gaussian s3->rotate 17->gamma 0.8), 256x1024x1024x3 f32"
@@ -329,6 +330,159 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------- other workloads
+def _ragged_sizes(n, seed):
+    import math
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(64), math.log(2048)
+    return [(int(round(math.exp(rng.uniform(lo, hi)))), int(round(math.exp(rng.uniform(lo, hi)))))
+            for _ in range(n)]
+
+
+def run_ragged(args):
+    """1000 RGB images, H and W log-uniform in [64, 2048]; per image rotate
+    U(-45,45), gaussian sigma U(0.5,4), gamma U(0.5,2), brightness U(-0.2,0.2),
+    fliplr p=0.5 (seeded counter RNG); one fused plan over the ragged batch."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from millipyde_gb300 import _abi
+    L = _abi.lib()
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.Stream(device=dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    n = args.images if args.images != N_IMG_DEFAULT else 1000
+    sizes = _ragged_sizes(n, SEED)
+    px = sum(h * w for h, w in sizes)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(SEED)
+    keep, ins, outs = [], [], []
+    with torch.cuda.stream(stream):
+        for h, w in sizes:
+            pitch = (w * 3 * 4 + 15) // 16 * 16
+            t = torch.rand((h, pitch // 4), device=dev, generator=gen)
+            o = torch.empty((h, pitch // 4), device=dev)
+            keep += [t, o]
+            ins.append(_abi.image(t.data_ptr(), h, w, 3, pitch))
+            outs.append(_abi.image(o.data_ptr(), h, w, 3, pitch))
+    stream.synchronize()
+    st = _abi.stages(_abi.stage("rotate", random=True, lo=(-45,), hi=(45,)),
+                     _abi.stage("gaussian", random=True, lo=(0.5,), hi=(4.0,)),
+                     _abi.stage("adjust_gamma", random=True, lo=(0.5, 1.0), hi=(2.0, 1.0)),
+                     _abi.stage("brightness", random=True, lo=(-0.2,), hi=(0.2,)),
+                     _abi.stage("fliplr", probability=0.5))
+    ia, oa = _abi.images(ins), _abi.images(outs)
+    plan = C.c_void_p()
+    _abi.check(L.mpk_plan_create(st, 5, ia, oa, n, SEED, 0, sp, C.byref(plan)))
+    nl = L.mpk_plan_num_launches(plan)
+    stream.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        _abi.check(L.mpk_plan_launch(plan, C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    for _ in range(max(3, args.warmup)):
+        g.replay()
+    clocks = Clocks()
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(args.steps):
+            g.replay()
+        e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        _abi.check(L.mpk_pipeline_run_unfused(st, 5, ia, oa, n, SEED, 0, sp))
+        e1.record(stream)
+    e1.synchronize()
+    po_ms = e0.elapsed_time(e1)
+    L.mpk_plan_destroy(plan)
+    peak, pk = measured_peaks()
+    gbs = px * 24 / (ms / 1e3) / 1e9
+    print(json.dumps({"metric": "Mpix/s fused ragged augmentation fwd", "value": round(px / 1e6 / (ms / 1e3), 1),
+                      "unit": "Mpix/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "ragged: %d RGB images, H,W log-uniform [64,2048], rotate U(-45,45) "
+                                             "-> gaussian U(0.5,4) -> gamma U(0.5,2) -> brightness U(-0.2,0.2) "
+                                             "-> fliplr p=0.5" % n, "pixels": px},
+                      "per_op": {"value": round(px / 1e6 / (po_ms / 1e3), 1), "unit": "Mpix/s"},
+                      "pipeline_hbm": {"bytes_per_px": 24, "achieved_gbs": round(gbs, 1),
+                                       "frac": round(gbs / peak, 4), "peak_source": pk},
+                      "gpu_launches": args.steps * nl, "clocks": clk}), flush=True)
+
+
+def run_grad(args, which):
+    """Differentiable fwd+bwd.  grad4: 64 x 512x512x3, rotate U(-30,30) ->
+    gaussian U(1,3) -> gamma U(0.7,1.5) -> rgb2grey, loss sum(out*W).
+    grad5: 16 x 8192x8192x3, gaussian 8 -> rotate U(-45,45) -> brightness
+    U(-0.1,0.1); backward recomputes the forward."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from millipyde_gb300.autograd import pipeline
+    dev = torch.device("cuda:0")
+    torch.manual_seed(SEED)
+    if which == "grad4":
+        B, Hh, Ww = (args.images if args.images != N_IMG_DEFAULT else 64), 512, 512
+        theta = (torch.rand(B, dtype=torch.float64, device=dev) * 60 - 30).requires_grad_()
+        sigma = (1 + 2 * torch.rand(B, dtype=torch.float64, device=dev)).requires_grad_()
+        gamma = (0.7 + 0.8 * torch.rand(B, dtype=torch.float64, device=dev)).requires_grad_()
+        ops = [("rotate", theta), ("gaussian", sigma), ("adjust_gamma", gamma), ("rgb2grey",)]
+        params = [theta, sigma, gamma]
+        bpp, wshape = 44, (B, Hh, Ww)
+        desc = "64 x 512x512x3, rotate U(-30,30) -> gaussian U(1,3) -> gamma U(0.7,1.5) -> rgb2grey"
+    else:
+        B, Hh, Ww = (args.images if args.images != N_IMG_DEFAULT else 16), 8192, 8192
+        theta = (torch.rand(B, dtype=torch.float64, device=dev) * 90 - 45).requires_grad_()
+        delta = (torch.rand(B, dtype=torch.float64, device=dev) * 0.2 - 0.1).requires_grad_()
+        ops = [("gaussian", 8.0), ("rotate", theta), ("brightness", delta)]
+        params = [theta, delta]
+        bpp, wshape = 60, (B, Hh, Ww, 3)
+        desc = "16 x 8192x8192x3, gaussian 8 -> rotate U(-45,45) -> brightness U(-0.1,0.1)"
+    x = torch.rand(B, Hh, Ww, 3, device=dev, requires_grad=True)
+    Wt = torch.randn(wshape, device=dev)
+
+    def step():
+        for p in [x] + params:
+            p.grad = None
+        y = pipeline(x, ops)
+        y.backward(Wt)          # d(sum(y * W))/dy = W
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    torch.cuda.reset_peak_memory_stats()
+    clocks = Clocks()
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    e1.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    px = B * Hh * Ww
+    peak, pk = measured_peaks()
+    gbs = px * bpp / (ms / 1e3) / 1e9
+    print(json.dumps({"metric": "Mpix/s fwd+bwd differentiable chain", "value": round(px / 1e6 / (ms / 1e3), 1),
+                      "unit": "Mpix/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": desc, "loss": "sum(out * W), W ~ N(0,1)"},
+                      "pipeline_hbm": {"bytes_per_px": bpp, "achieved_gbs": round(gbs, 1),
+                                       "frac": round(gbs / peak, 4), "peak_source": pk},
+                      "torch_peak_memory_gb": round(torch.cuda.max_memory_allocated() / 1e9, 2),
+                      "clocks": clk}), flush=True)
+
+
 def main():
     global N_IMG
     ap = argparse.ArgumentParser()
@@ -340,11 +494,18 @@ def main():
                     help="batch size (profiling runs use a smaller batch)")
     ap.add_argument("--legs", default="all", choices=["all", "fused"],
                     help="'fused' times only the fused plan (profiling runs)")
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "ragged", "grad4", "grad5"],
+                    help="uniform: the headline batch; the others are the ragged, "
+                         "differentiable and large-image configurations")
     args = ap.parse_args()
     N_IMG = args.images
     CONFIG["images"] = N_IMG
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ragged":
+        run_ragged(args)
+    elif args.workload in ("grad4", "grad5"):
+        run_grad(args, args.workload)
     else:
         run_ours(args)
 
