@@ -328,6 +328,25 @@ MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, const MPImage
                                const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
                                void *stream);
 
+/* Allocation-free batch.  No counterpart in the reference.  For callers that
+ * cannot allocate device memory (GPU memory owned by another allocator or
+ * reserved up front, or a loop where a cudaMalloc would stall): the same
+ * stages as mpk_pipeline_run on caller-provided device buffers (in[i] ->
+ * out[i], geometry from mpk_pipeline_shapes), allocating no device memory:
+ * no cudaMalloc, no cudaFree, no device-allocating library routine (job
+ * descriptors travel as kernel parameters).  Intermediates live in a 32 MB
+ * file-scope device array (two 16 MB halves) that every GPU loading the
+ * library holds until exit; any image whose intermediate would exceed 16 MB
+ * is rejected with MP_ERROR_TOO_LARGE before anything is launched.  Images
+ * run one after another on `stream`; the call returns when they are done.
+ * Its first call on a device resolves the array's device address (set-up,
+ * with that device current).  Every call uses the same array, so calls that
+ * overlap on the GPU (other threads or streams) race; stale contents from an
+ * earlier call are never read. */
+MPStatus mpk_pipeline_run_noalloc(const MPStage *stages, int nstages, const MPImage *in,
+                                  const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
+                                  void *stream);
+
 /* Object-level batch used by Pipeline.run: applies the stages in place to
  * each object (float32 images: fused path when fused != 0, else one launch
  * per stage and image; other dtypes: the per-op entry points).  Image i uses

@@ -123,6 +123,8 @@ SIGNATURES = {
                                    C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "mpk_pipeline_run_host": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
                                     C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64, _P]),
+    "mpk_pipeline_run_noalloc": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
+                                       C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64, _P]),
     "mpk_pipeline_run_objects": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(C.POINTER(MPObjData)),
                                        C.c_int, C.c_uint64, C.c_uint64, C.c_int]),
     "mpk_pipeline_produce": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(C.POINTER(MPObjData)),

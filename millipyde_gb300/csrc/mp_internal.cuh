@@ -227,6 +227,13 @@ MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem_bytes, cudaStr
 enum { MPK_POINT_ADJ = 10, MPK_ROTATE_ADJ = 11 };
 MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
                            int *err, cudaStream_t s);
+// Single-job launch with an explicit device error word (no allocation).
+MPStatus mp_launch_single_err(int kind, const MPJob &job, size_t smem_bytes, int *err, cudaStream_t s);
+// Runs the stages on one image, intermediates in the two caller-provided
+// device buffers of half_bytes each; allocates no device memory.
+MPStatus mp_run_image_noalloc(const MPStage *stages, int nstages, uint64_t seed, uint64_t index,
+                              const MPImage &in, const MPImage &out, void *half0, void *half1,
+                              size_t half_bytes, int *err, cudaStream_t s);
 // In-place channel-agnostic pointwise list over n contiguous floats.
 MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s);
 // Dynamic shared memory a GAUSS launch needs for the given geometry.

@@ -604,6 +604,24 @@ MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem, cudaStream_t 
         cudaLaunchKernel(fn, dim3(job.ntiles), dim3(MP_THREADS), args, smem, s));
 }
 
+// Single-job launch reporting into a caller-supplied device error word
+// (allocation-free path: nothing here allocates device memory).
+MPStatus mp_launch_single_err(int kind, const MPJob &job, size_t smem, int *err, cudaStream_t s)
+{
+    if (job.ntiles <= 0) return MILLIPYDE_SUCCESS;
+    const void *fn;
+    switch (kind) {
+    case MPK_GAUSS: fn = (const void *)mp_gauss_single; break;
+    case MPK_ROTATE: fn = (const void *)mp_rotate_single; break;
+    case MPK_TRANSPOSE: fn = (const void *)mp_transpose_single; break;
+    default: fn = (const void *)mp_point_single; break;
+    }
+    MPStatus st = mp_prepare_smem(fn, smem);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    void *args[] = {(void *)&job, (void *)&err};
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(job.ntiles), dim3(MP_THREADS), args, smem, s));
+}
+
 MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s)
 {
     if (n == 0) return MILLIPYDE_SUCCESS;

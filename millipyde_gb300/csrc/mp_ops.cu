@@ -1479,3 +1479,54 @@ extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *p
     mp_free_async(scratch, s);
     return st;
 }
+
+// ---------------------------------------------------------------------------
+// One image through its segments with caller-provided intermediate buffers
+// (used by the allocation-free entry point in mp_noalloc.cu).
+// ---------------------------------------------------------------------------
+MPStatus mp_run_image_noalloc(const MPStage *stages, int nstages, uint64_t seed, uint64_t index,
+                              const MPImage &in, const MPImage &out, void *half0, void *half1,
+                              size_t half_bytes, int *err, cudaStream_t s)
+{
+    if (in.channels != 1 && in.channels != 3 && in.channels != 4) return MP_ERROR_BAD_DESCRIPTOR;
+    if (in.height < 0 || in.width < 0 || (in.pitch % 4) ||
+        ((long long)in.width * in.channels * 4 > in.pitch && in.height > 0))
+        return MP_ERROR_BAD_DESCRIPTOR;
+    std::vector<ROp> ops;
+    MPStatus st = mp_resolve_image(stages, nstages, seed, index, ops, nullptr);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    std::vector<Seg> segs;
+    mp_segment(ops, in.channels, in.height, in.width, segs);
+    const Seg &last = segs.back();
+    if (out.height != last.hout || out.width != last.wout || out.channels != last.cout ||
+        out.pitch < last.wout * last.cout * 4 || (out.pitch % 4) ||
+        (!out.data && (long long)last.hout * last.wout > 0))
+        return MP_ERROR_BAD_DESCRIPTOR;
+    // every intermediate must fit its half before anything is launched
+    for (size_t k = 0; k + 1 < segs.size(); ++k) {
+        const size_t need = (size_t)segs[k].hout * mp_round16((long long)segs[k].wout * segs[k].cout * 4);
+        if (need > half_bytes) return MP_ERROR_TOO_LARGE;
+    }
+    MPImage cur = in;
+    for (size_t k = 0; k < segs.size(); ++k) {
+        MPImage dst;
+        if (k + 1 == segs.size()) {
+            dst = out;
+        } else {
+            dst.height = segs[k].hout;
+            dst.width = segs[k].wout;
+            dst.channels = segs[k].cout;
+            dst.pitch = mp_round16((long long)dst.width * dst.channels * 4);
+            dst.data = (k % 2 == 0) ? half0 : half1;
+        }
+        int tw, th;
+        mp_seg_tiles(segs[k], &tw, &th);
+        MPJob J;
+        st = mp_fill_job(J, segs[k], cur, dst, tw, th);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        st = mp_launch_single_err(segs[k].kind, J, mp_seg_smem(segs[k], tw, th), err, s);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        cur = dst;
+    }
+    return MILLIPYDE_SUCCESS;
+}
