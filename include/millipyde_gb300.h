@@ -233,6 +233,8 @@ void mpdev_set_target_device(int device_id);
 MPBool mpdev_is_valid_device(int device_id);
 void *mpdev_get_stream(int device_id, int stream_id);
 MPStatus mpdev_synchronize(void);
+/* Device name (e.g. "NVIDIA GB300") into buf (len bytes, NUL-terminated). */
+MPStatus mpdev_get_device_name(int device_id, char *buf, int len);
 MPStatus mpdev_stream_synchronize(void *stream);
 
 /* ------------------------------------------------------------------------ */
@@ -327,6 +329,30 @@ MPStatus mpk_plan_launch_info(const MPPlan *plan, int i, int *kind, int *njobs, 
 MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, const MPImage *in,
                                const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
                                void *stream);
+
+/* Autotuning: tile size (tw x th output pixels, multiples of 8) of the
+ * gaussian kernel for a channel variant (source channels, channels after the
+ * prologue), prologue flag and radius range; the planner prefers these over
+ * its built-in table.  millipyde_gb300/autotune.py times candidates on the
+ * device and records the fastest.  get returns what the planner would use. */
+MPStatus mpk_tune_set_gauss_tile(int cin, int cmid, int has_pro, int radius_lo, int radius_hi,
+                                 int tw, int th);
+MPStatus mpk_tune_get_gauss_tile(int cin, int cmid, int has_pro, int radius, int *tw, int *th);
+void mpk_tune_clear(void);
+
+/* Differentiable chains on dense batches (the autograd path): B images of
+ * H x W x C float32, packed rows, image b at x + b*H*W*C; ops[nops] MPOpCode;
+ * params[(b*nops + k)*3 + j] explicit per-image parameters (host memory).
+ * forward writes y (geometry from mpk_chain_shape); backward recomputes the
+ * forward intermediates in image chunks, writes dx and ADDS parameter
+ * gradients (FP64) to dparams[(b*nops + k)*3 + j] (device memory, zeroed by
+ * the caller). */
+MPStatus mpk_chain_shape(const int *ops, int nops, int H, int W, int C, int *Ho, int *Wo, int *Co);
+MPStatus mpk_chain_forward(const int *ops, int nops, const double *params, const float *x, float *y,
+                           int B, int H, int W, int C, void *stream);
+MPStatus mpk_chain_backward(const int *ops, int nops, const double *params, const float *x,
+                            const float *dy, float *dx, double *dparams, int B, int H, int W, int C,
+                            void *stream);
 
 /* Allocation-free batch.  No counterpart in the reference.  For callers that
  * cannot allocate device memory (GPU memory owned by another allocator or

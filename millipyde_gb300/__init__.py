@@ -38,6 +38,13 @@ except ImportError as e:  # pragma: no cover - exercised only without a build
 
 from ._io import image_from_path, images_from_path  # noqa: E402,F401
 
+try:  # tuned gaussian tiles for this GPU (no-op without a GPU or a table)
+    from . import autotune as _autotune
+
+    _autotune.load()
+except (OSError, ValueError, KeyError):  # pragma: no cover
+    pass
+
 LIBRARY_PATH = _os.path.join(_os.path.dirname(__file__), "libmillipyde_gb300.so")
 
 __all__ = [

@@ -106,6 +106,7 @@ SIGNATURES = {
     "mpdev_is_valid_device": (C.c_int, [C.c_int]),
     "mpdev_get_stream": (_P, [C.c_int, C.c_int]),
     "mpdev_synchronize": (_ST, []),
+    "mpdev_get_device_name": (_ST, [C.c_int, C.c_char_p, C.c_int]),
     "mpdev_stream_synchronize": (_ST, [_P]),
     "mpk_pipeline_shapes": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
                                   C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64]),
@@ -123,6 +124,16 @@ SIGNATURES = {
                                    C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "mpk_pipeline_run_host": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
                                     C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64, _P]),
+    "mpk_tune_set_gauss_tile": (_ST, [C.c_int] * 7),
+    "mpk_tune_get_gauss_tile": (_ST, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int)]),
+    "mpk_tune_clear": (None, []),
+    "mpk_chain_shape": (_ST, [C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int, C.c_int,
+                              C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mpk_chain_forward": (_ST, [C.POINTER(C.c_int), C.c_int, _P, _P, _P, C.c_int, C.c_int, C.c_int,
+                                C.c_int, _P]),
+    "mpk_chain_backward": (_ST, [C.POINTER(C.c_int), C.c_int, _P, _P, _P, _P, _P, C.c_int, C.c_int,
+                                 C.c_int, C.c_int, _P]),
     "mpk_pipeline_run_noalloc": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
                                        C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64, _P]),
     "mpk_pipeline_run_objects": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(C.POINTER(MPObjData)),

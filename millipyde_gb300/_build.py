@@ -25,7 +25,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 
-CU_SOURCES = ["mp_runtime.cu", "mp_kernels.cu", "mp_ops.cu", "mp_grad.cu", "mp_noalloc.cu"]
+CU_SOURCES = ["mp_runtime.cu", "mp_kernels.cu", "mp_ops.cu", "mp_grad.cu", "mp_noalloc.cu", "mp_legacy.cu"]
 C_SOURCES = ["py_module.c", "py_objects.c", "py_compose.c"]
 HEADERS = ["mp_internal.cuh", "py_common.h"]
 

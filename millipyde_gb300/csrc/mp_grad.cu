@@ -25,17 +25,6 @@
 #define MP_THREADS 256
 #define MP_DEG2RAD_F 0.01745329252f
 
-__device__ __forceinline__ int mp_find_job_adj(const MPJob *__restrict__ jobs, int njobs, int tile)
-{
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].tile0 <= tile) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 __device__ __forceinline__ float mp_block_sum(float v, float *red)
 {
 #pragma unroll
@@ -97,11 +86,11 @@ __device__ __forceinline__ void mp_pw_back(const PwOp &o, const float v[4], int 
                 const float x = v[k];
                 float d = 0.0f;
                 if (x > 0.0f) {
-                    const float pw = powf(x, o.p0);
+                    const float pw = __powf(x, o.p0);
                     const float t = o.p1 * pw;
                     if (t > 0.0f && t < 1.0f) {
                         d = g[k] * o.p0 * t / x;
-                        pa[0] += g[k] * t * logf(x);
+                        pa[0] += g[k] * t * __logf(x);
                         pa[1] += g[k] * pw;
                     }
                 }
@@ -277,33 +266,31 @@ __device__ void mp_rotate_adj_tile(const MPJob &J, int t, float *red)
 }
 
 __global__ void __launch_bounds__(MP_THREADS) mp_point_adjoint_batch(const MPJob *__restrict__ jobs,
-                                                                     int njobs, int *err)
+                                                                     const int *__restrict__ tile_job,
+                                                                     int *err)
 {
     __shared__ float red[32];
     const int t = blockIdx.x;
-    const MPJob &J = jobs[mp_find_job_adj(jobs, njobs, t)];
-    const int lt = t - J.tile0;
-    if (lt >= J.ntiles) return;
-    mp_point_adj_tile(J, lt, red);
+    const MPJob &J = jobs[__ldg(tile_job + t)];
+    mp_point_adj_tile(J, t - J.tile0, red);
 }
 
 __global__ void __launch_bounds__(MP_THREADS) mp_rotate_adjoint_batch(const MPJob *__restrict__ jobs,
-                                                                      int njobs, int *err)
+                                                                      const int *__restrict__ tile_job,
+                                                                      int *err)
 {
     __shared__ float red[32];
     const int t = blockIdx.x;
-    const MPJob &J = jobs[mp_find_job_adj(jobs, njobs, t)];
-    const int lt = t - J.tile0;
-    if (lt >= J.ntiles) return;
-    mp_rotate_adj_tile(J, lt, red);
+    const MPJob &J = jobs[__ldg(tile_job + t)];
+    mp_rotate_adj_tile(J, t - J.tile0, red);
 }
 
-MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, int njobs, int total_tiles, int *err,
-                           cudaStream_t s)
+MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, const int *tile_job, int total_tiles,
+                           int *err, cudaStream_t s)
 {
-    if (total_tiles <= 0 || njobs <= 0) return MILLIPYDE_SUCCESS;
+    if (total_tiles <= 0) return MILLIPYDE_SUCCESS;
     const void *fn = kind == MPK_ROTATE_ADJ ? (const void *)mp_rotate_adjoint_batch
                                             : (const void *)mp_point_adjoint_batch;
-    void *args[] = {(void *)&jobs_dev, (void *)&njobs, (void *)&err};
+    void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&err};
     return mp_cuda_status(cudaLaunchKernel(fn, dim3(total_tiles), dim3(MP_THREADS), args, 0, s));
 }

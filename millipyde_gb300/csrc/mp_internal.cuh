@@ -40,7 +40,7 @@ struct PwList {
 // struct 128-byte aligned, so every entry of a job table in global memory
 // holds a legal TMA descriptor address.
 struct MPJob {
-    CUtensorMap tmap;          // GAUSS: 2-D map over the source, box {64, th+2r}
+    CUtensorMap tmap;          // GAUSS: 2-D map over the source, box {64, th + 2r}
     const float *src;
     float *dst;
     long long cosq, sinq;      // ROTATE: cos/sin * 2^(MP_FIX_FRAC-1), rounded
@@ -76,41 +76,73 @@ struct MPJob {
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float mp_clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
 
+// One pointwise op on v[0..c-1]; returns the new channel count.
+__device__ __forceinline__ int mp_pw_op(int op, float p0, float p1, float p2, float v[4], int c)
+{
+    const int cc = (c == 4) ? 3 : c;     // colour channels
+    switch (op) {
+    case MP_OP_RGB2GREY:
+        if (c >= 3) {
+            v[0] = fminf(1.0f, 0.2125f * v[0] + 0.7154f * v[1] + 0.0721f * v[2]);
+            c = 1;
+        }
+        break;
+    case MP_OP_BRIGHTNESS:
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (k < cc) v[k] = mp_clamp01(v[k] + p0);
+        break;
+    case MP_OP_ADJUST_GAMMA:
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (k < cc) v[k] = mp_clamp01(p1 * __powf(v[k], p0));
+        break;
+    case MP_OP_COLORIZE:
+        if (c >= 3) {
+            v[0] = fminf(1.0f, v[0] * p0);
+            v[1] = fminf(1.0f, v[1] * p1);
+            v[2] = fminf(1.0f, v[2] * p2);
+        }
+        break;
+    default:
+        break;
+    }
+    return c;
+}
+
 // Applies L to v[0..c-1] and returns the new channel count.
 __device__ __forceinline__ int mp_pw_apply(const PwList &L, float v[4], int c)
 {
     for (int i = 0; i < L.n; ++i) {
         const PwOp o = L.op[i];
-        const int cc = (c == 4) ? 3 : c;     // colour channels
-        switch (o.op) {
-        case MP_OP_RGB2GREY:
-            if (c >= 3) {
-                v[0] = fminf(1.0f, 0.2125f * v[0] + 0.7154f * v[1] + 0.0721f * v[2]);
-                c = 1;
-            }
-            break;
-        case MP_OP_BRIGHTNESS:
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                if (k < cc) v[k] = mp_clamp01(v[k] + o.p0);
-            break;
-        case MP_OP_ADJUST_GAMMA:
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                if (k < cc) v[k] = mp_clamp01(o.p1 * powf(v[k], o.p0));
-            break;
-        case MP_OP_COLORIZE:
-            if (c >= 3) {
-                v[0] = fminf(1.0f, v[0] * o.p0);
-                v[1] = fminf(1.0f, v[1] * o.p1);
-                v[2] = fminf(1.0f, v[2] * o.p2);
-            }
-            break;
-        default:
-            break;
-        }
+        c = mp_pw_op(o.op, o.p0, o.p1, o.p2, v, c);
     }
     return c;
+}
+
+// A pointwise list with its first op held in registers: lists of one op (the
+// common prologue / epilogue) run without reading the list per pixel.
+struct PwFast {
+    int n, op;
+    float p0, p1, p2;
+};
+
+__device__ __forceinline__ PwFast mp_pw_fast(const PwList &L)
+{
+    PwFast f;
+    f.n = L.n;
+    f.op = L.n ? L.op[0].op : 0;
+    f.p0 = L.n ? L.op[0].p0 : 0.f;
+    f.p1 = L.n ? L.op[0].p1 : 0.f;
+    f.p2 = L.n ? L.op[0].p2 : 0.f;
+    return f;
+}
+
+__device__ __forceinline__ int mp_pw_apply_f(const PwFast &f, const PwList &L, float v[4], int c)
+{
+    if (f.n == 0) return c;
+    if (f.n == 1) return mp_pw_op(f.op, f.p0, f.p1, f.p2, v, c);
+    return mp_pw_apply(L, v, c);
 }
 
 // ---------------------------------------------------------------------------
@@ -216,16 +248,21 @@ void mp_free_async(void *p, cudaStream_t s);
 
 // Kernel launchers (mp_kernels.cu).  `jobs` is a device table of njobs jobs
 // sorted by tile0; `total_tiles` the sum of their ntiles.
-MPStatus mp_launch_kind(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
-                        size_t smem_bytes, int *err, cudaStream_t s);
-// Sets the dynamic shared-memory limit a (kind, smem) launch needs; call
-// outside stream capture.
-MPStatus mp_prepare_kind(int kind, size_t smem_bytes);
+// `tile_job[t]` is the job index of global tile t; `variant` selects the
+// channel specialisation (mp_variant) of GAUSS / ROTATE launches.
+// `gauss` = {tw, th, rmax, use_tma} for GAUSS launches (persistent grid).
+MPStatus mp_launch_kind(int kind, int variant, const MPJob *jobs_dev, const int *tile_job,
+                        int total_tiles, size_t smem_bytes, int *err, cudaStream_t s,
+                        const int *gauss = nullptr);
+// Sets the dynamic shared-memory limit a launch needs; call outside capture.
+MPStatus mp_prepare_kind(int kind, int variant, size_t smem_bytes);
+// Channel variant of a (source channels, channels after prologue) pair, -1 if none.
+int mp_variant(int cin, int cmid);
 // Single-job launch with the job passed by value (no device table).
 MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem_bytes, cudaStream_t s);
 // Adjoint kernels (mp_grad.cu), one job per image, tiles as the forward kinds.
 enum { MPK_POINT_ADJ = 10, MPK_ROTATE_ADJ = 11 };
-MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
+MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, const int *tile_job, int total_tiles,
                            int *err, cudaStream_t s);
 // Single-job launch with an explicit device error word (no allocation).
 MPStatus mp_launch_single_err(int kind, const MPJob &job, size_t smem_bytes, int *err, cudaStream_t s);
@@ -234,6 +271,9 @@ MPStatus mp_launch_single_err(int kind, const MPJob &job, size_t smem_bytes, int
 MPStatus mp_run_image_noalloc(const MPStage *stages, int nstages, uint64_t seed, uint64_t index,
                               const MPImage &in, const MPImage &out, void *half0, void *half1,
                               size_t half_bytes, int *err, cudaStream_t s);
+// The reference's own layouts (uint8 RGBA / uint8 RGB for rgb2grey /
+// float64 greyscale) and arithmetic, in place on an object (mp_legacy.cu).
+MPStatus mp_legacy_apply(MPObjData *o, int op, double p0, double p1, double p2);
 // In-place channel-agnostic pointwise list over n contiguous floats.
 MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s);
 // Dynamic shared memory a GAUSS launch needs for the given geometry.

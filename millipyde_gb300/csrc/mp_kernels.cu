@@ -9,7 +9,9 @@
 //   TRANSPOSE  out[x][y] = in[y][x]                 (src/millipyde_image.cpp:73-96)
 // Every kernel reads its work from an MPJob (one per image).  A launch covers
 // a ragged batch: blockIdx.x is a global tile index, mapped to its image by a
-// binary search over the jobs' tile offsets.
+// per-tile job index built with the plan.  GAUSS and ROTATE are compiled per
+// channel variant (source channels, channels after the prologue).
+#include <algorithm>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -17,20 +19,6 @@
 #include "mp_internal.cuh"
 
 #define MP_THREADS 256
-
-// ---------------------------------------------------------------------------
-// Job lookup
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int mp_find_job(const MPJob *__restrict__ jobs, int njobs, int tile)
-{
-    int lo = 0, hi = njobs - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].tile0 <= tile) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
 
 // ---------------------------------------------------------------------------
 // GAUSS shared-memory layout (host and device agree on it).
@@ -71,7 +59,6 @@ __host__ __device__ __forceinline__ GaussGeom mp_gauss_geom(int tw, int th, int 
         A = S > ob ? S : ob;
         B = vT;
     }
-    // mbarrier, vertical taps, horizontal taps, 32-float reduction scratch
     const int head = mp_round_up(16 + 8 * mp_round_up(MP_MAX_TAPS, 16) + 4 * 32, 128);
     g.offA = head;
     g.offB = g.offA + mp_round_up(A * 4, 128);
@@ -131,6 +118,15 @@ __device__ __forceinline__ void mp_conv8(const float *base, int stride, int ntap
     }
 }
 
+// Channel-count variants the GAUSS and ROTATE kernels are compiled for:
+// (source channels, channels after the prologue).
+template <int V> struct MPChan;
+template <> struct MPChan<0> { static constexpr int CIN = 1, CMID = 1; };
+template <> struct MPChan<1> { static constexpr int CIN = 3, CMID = 3; };
+template <> struct MPChan<2> { static constexpr int CIN = 4, CMID = 4; };
+template <> struct MPChan<3> { static constexpr int CIN = 3, CMID = 1; };
+template <> struct MPChan<4> { static constexpr int CIN = 4, CMID = 1; };
+
 // One output tile (tw x th pixels) of a separable gaussian.
 //   1. TMA loads the halo'd source tile (th+2r rows, (tw+2r)*cin floats plus
 //      up to 3 floats of 16-byte alignment slack) as nbx boxes of 64 floats;
@@ -138,16 +134,21 @@ __device__ __forceinline__ void mp_conv8(const float *base, int stride, int ntap
 //   2. Optional prologue: pointwise ops into G (zeros kept outside the image).
 //   3. Vertical pass -> vT, stored transposed ([column][row]).
 //   4. Horizontal pass over vT rows -> obuf ([row][x*cmid+c]).
-//   5. Copy-out with epilogue and the fliplr map.
+//   5. Copy-out with epilogue and the fliplr map (or, in dot mode, the sum of
+//      out * aux over the tile).
+// Loops over 2-D index ranges run warp-per-row / lane-per-column, so no
+// integer division sits in a per-element loop.
+template <int CIN, int CMID>
 __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned char *smem_raw,
                                               bool map_in_global, int *err)
 {
     const int r = J.radius, tw = J.tw, th = J.th;
-    const int cin = J.cin, cmid = J.cmid;
+    const int H = J.h, W = J.w;
     const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
     const int x0 = tx * tw, y0 = ty * th;
     const int has_pro = J.pro.n > 0;
-    const GaussGeom g = mp_gauss_geom(tw, th, r, cin, cmid, has_pro);
+    const GaussGeom g = mp_gauss_geom(tw, th, r, CIN, CMID, has_pro);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
 
     unsigned char *base =
         smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
@@ -159,11 +160,12 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
     float *B = reinterpret_cast<float *>(base + g.offB);
     float *S = A;
 
-    const int gx = (x0 - r) * cin;
+    const int gx = (x0 - r) * CIN;
     const int xa = gx & ~3;
     const int delta = gx - xa;
-    const int nbx = (delta + (tw + 2 * r) * cin + 63) / 64;
+    const int nbx = (delta + (tw + 2 * r) * CIN + 63) / 64;
     const int ntaps = 2 * r + 1;
+    const int boxs = 64 * g.BH;           // floats per TMA box
 
     for (int i = threadIdx.x; i < ntaps; i += blockDim.x) {
         wsm[i] = J.wts[i];
@@ -178,9 +180,9 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
         __syncthreads();
         if (threadIdx.x == 0) {
             if (map_in_global) mp_tensormap_acquire(&J.tmap);
-            mp_mbar_arrive_expect_tx(bar, (uint32_t)(nbx * 64 * g.BH * 4));
+            mp_mbar_arrive_expect_tx(bar, (uint32_t)(nbx * boxs * 4));
             for (int b = 0; b < nbx; ++b)
-                mp_tma_load_2d(S + b * 64 * g.BH, &J.tmap, bar, xa + 64 * b, y0 - r);
+                mp_tma_load_2d(S + b * boxs, &J.tmap, bar, xa + 64 * b, y0 - r);
         }
         const bool ok = mp_mbar_wait_bounded(bar, 0);
         if (!__syncthreads_and(ok)) {
@@ -191,18 +193,20 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
     } else {
         // Plain-load fallback for sources whose rows are not 16-byte aligned:
         // same box-major layout, zeros outside the image.
-        const int rowlen = J.w * cin;
-        const int n = nbx * 64 * g.BH;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const int b = i / (64 * g.BH);
-            const int rem = i - b * 64 * g.BH;
-            const int row = rem >> 6, col = rem & 63;
-            const int gyy = y0 - r + row;
-            const int gxx = xa + 64 * b + col;
-            float v = 0.0f;
-            if (gyy >= 0 && gyy < J.h && gxx >= 0 && gxx < rowlen)
-                v = __ldg(J.src + (size_t)gyy * J.src_pitch + gxx);
-            S[i] = v;
+        const int rowlen = W * CIN;
+        const float *src = J.src;
+        const int sp = J.src_pitch;
+        for (int b = 0; b < nbx; ++b) {
+            for (int row = warp; row < g.BH; row += nwarps) {
+                const int gyy = y0 - r + row;
+                const bool rowin = gyy >= 0 && gyy < H;
+                for (int col = lane; col < 64; col += 32) {
+                    const int gxx = xa + 64 * b + col;
+                    float v = 0.0f;
+                    if (rowin && gxx >= 0 && gxx < rowlen) v = __ldg(src + (size_t)gyy * sp + gxx);
+                    S[b * boxs + row * 64 + col] = v;
+                }
+            }
         }
         __syncthreads();
     }
@@ -215,23 +219,26 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
     if (has_pro) {
         float *G = B;
         const int npx = tw + 2 * r;
-        for (int i = threadIdx.x; i < g.BH * npx; i += blockDim.x) {
-            const int row = i / npx, xi = i - row * npx;
-            const int gyy = y0 - r + row, gxx = x0 - r + xi;
-            float v[4] = {0.f, 0.f, 0.f, 0.f};
-            if (gyy >= 0 && gyy < J.h && gxx >= 0 && gxx < J.w) {
+        const PwFast pro = mp_pw_fast(J.pro);
+        for (int row = warp; row < g.BH; row += nwarps) {
+            const int gyy = y0 - r + row;
+            const bool rowin = gyy >= 0 && gyy < H;
+            const float *Srow = S + row * 64;
+            float *Grow = G + row * g.GWp;
+            for (int xi = lane; xi < npx; xi += 32) {
+                const int gxx = x0 - r + xi;
+                float v[4] = {0.f, 0.f, 0.f, 0.f};
+                if (rowin && gxx >= 0 && gxx < W) {
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    if (c < cin) {
-                        const int col = delta + xi * cin + c;
-                        v[c] = S[(col >> 6) * 64 * g.BH + row * 64 + (col & 63)];
+                    for (int c = 0; c < CIN; ++c) {
+                        const int col = delta + xi * CIN + c;
+                        v[c] = Srow[(col >> 6) * boxs + (col & 63)];
                     }
+                    mp_pw_apply_f(pro, J.pro, v, CIN);
                 }
-                mp_pw_apply(J.pro, v, cin);
-            }
 #pragma unroll
-            for (int c = 0; c < 4; ++c)
-                if (c < cmid) G[row * g.GWp + xi * cmid + c] = v[c];
+                for (int c = 0; c < CMID; ++c) Grow[xi * CMID + c] = v[c];
+            }
         }
         __syncthreads();
         vsrc = G;
@@ -252,10 +259,10 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
     // ---- 3. vertical pass: item (q, grp) = 4 columns x 8 output rows
     const int ngrp = th / 8;
     for (int it = threadIdx.x; it < nq * ngrp; it += blockDim.x) {
-        const int q = it % nq, grp = it / nq;
+        const int grp = it / nq, q = it - grp * nq;
         const float *colbase;
         if (has_pro) colbase = vsrc + 4 * q;
-        else colbase = vsrc + (q >> 4) * 64 * g.BH + ((q & 15) << 2);
+        else colbase = vsrc + (q >> 4) * boxs + ((q & 15) << 2);
         float4 acc[8];
 #pragma unroll
         for (int o = 0; o < 8; ++o) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -279,17 +286,16 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
 
     // ---- 4. horizontal pass: item (a, c, b) = 4 rows x 8 consecutive x, channel c
     const int na = th / 4, nb = tw / 8;
-    for (int it = threadIdx.x; it < na * cmid * nb; it += blockDim.x) {
-        const int a = it % na;
-        const int rest = it / na;
-        const int c = rest % cmid, b = rest / cmid;
+    for (int it = threadIdx.x; it < na * CMID * nb; it += blockDim.x) {
+        const int rest = it / na, a = it - rest * na;
+        const int b = rest / CMID, c = rest - b * CMID;
         float4 acc[8];
 #pragma unroll
         for (int o = 0; o < 8; ++o) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-        mp_conv8(vT + ((8 * b) * cmid + c) * g.RBp + 4 * a, cmid * g.RBp, ntaps, wsm_h, acc);
+        mp_conv8(vT + ((8 * b) * CMID + c) * g.RBp + 4 * a, CMID * g.RBp, ntaps, wsm_h, acc);
 #pragma unroll
         for (int o = 0; o < 8; ++o) {
-            float *dst = obuf + (4 * a) * g.OBW + (8 * b + o) * cmid + c;
+            float *dst = obuf + (4 * a) * g.OBW + (8 * b + o) * CMID + c;
             dst[0] = acc[o].x;
             dst[g.OBW] = acc[o].y;
             dst[2 * g.OBW] = acc[o].z;
@@ -301,88 +307,138 @@ __device__ __forceinline__ void mp_gauss_tile(const MPJob &J, int t, unsigned ch
     // ---- 5a. dot mode: sum(out * aux) over the tile into acc[0]
     if (J.dot) {
         float part = 0.f;
-        for (int i = threadIdx.x; i < th * tw; i += blockDim.x) {
-            const int tt = i / tw, xx = i - tt * tw;
-            const int gyy = y0 + tt, gxx = x0 + xx;
-            if (gyy >= J.h || gxx >= J.w) continue;
-            const float *d = J.aux + (size_t)gyy * J.aux_pitch + (size_t)gxx * cmid;
-            for (int c = 0; c < cmid; ++c) part = fmaf(obuf[tt * g.OBW + xx * cmid + c], d[c], part);
+        for (int tt = warp; tt < th; tt += nwarps) {
+            const int gyy = y0 + tt;
+            if (gyy >= H) break;
+            const float *arow = J.aux + (size_t)gyy * J.aux_pitch;
+            for (int xx = lane; xx < tw; xx += 32) {
+                const int gxx = x0 + xx;
+                if (gxx >= W) break;
+#pragma unroll
+                for (int c = 0; c < CMID; ++c)
+                    part = fmaf(obuf[tt * g.OBW + xx * CMID + c], arow[(size_t)gxx * CMID + c], part);
+            }
         }
         mp_block_add(part, red, J.acc);
         return;
     }
     // ---- 5. copy-out with epilogue and output map
-    for (int i = threadIdx.x; i < th * tw; i += blockDim.x) {
-        const int tt = i / tw, xx = i - tt * tw;
-        const int gyy = y0 + tt, gxx = x0 + xx;
-        if (gyy >= J.h || gxx >= J.w) continue;
-        float v[4];
+    const PwFast epi = mp_pw_fast(J.epi);
+    const int flip = J.flip, wo = J.wo;
+    float *dstb = J.dst;
+    const int dp = J.dst_pitch;
+    for (int tt = warp; tt < th; tt += nwarps) {
+        const int gyy = y0 + tt;
+        if (gyy >= H) break;
+        float *drow = dstb + (size_t)gyy * dp;
+        const float *orow = obuf + tt * g.OBW;
+        for (int xx = lane; xx < tw; xx += 32) {
+            const int gxx = x0 + xx;
+            if (gxx >= W) break;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int c = 0; c < 4; ++c) v[c] = (c < cmid) ? obuf[tt * g.OBW + xx * cmid + c] : 0.f;
-        const int co = mp_pw_apply(J.epi, v, cmid);
-        const int xo = J.flip ? (J.wo - 1 - gxx) : gxx;
-        float *dst = J.dst + (size_t)gyy * J.dst_pitch + (size_t)xo * co;
+            for (int c = 0; c < CMID; ++c) v[c] = orow[xx * CMID + c];
+            const int xo = flip ? (wo - 1 - gxx) : gxx;
+            if (epi.n == 0) {
+                float *d = drow + (size_t)xo * CMID;
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
-            if (c < co) dst[c] = v[c];
+                for (int c = 0; c < CMID; ++c) d[c] = v[c];
+            } else {
+                const int co = mp_pw_apply_f(epi, J.epi, v, CMID);
+                float *d = drow + (size_t)xo * co;
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    if (c < co) d[c] = v[c];
+            }
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
 // ROTATE: 32x32 output tile, 256 threads, 4 rows per thread.  Source
 // coordinates in 64-bit fixed point (MP_FIX_FRAC fractional bits), so the
-// bilinear fractions keep ~24 correct bits even for 8192-wide images.
+// bilinear fractions keep ~24 correct bits even for 8192-wide images; a
+// thread steps its coordinates exactly from one of its rows to the next.
 //   s = R(theta) (p - c) + c,  c = (W/2, H/2),  p = output pixel
 // Neighbours outside the source contribute 0 (zero fill); the prologue is
 // applied to each in-range neighbour before interpolation.
 // ---------------------------------------------------------------------------
+template <int CIN>
 __device__ __forceinline__ void mp_load_px(const MPJob &J, int ix, int iy, float v[4])
 {
     v[0] = v[1] = v[2] = v[3] = 0.f;
     if (ix < 0 || iy < 0 || ix >= J.w || iy >= J.h) return;
-    const float *p = J.src + (size_t)iy * J.src_pitch + (size_t)ix * J.cin;
+    const float *p = J.src + (size_t)iy * J.src_pitch + (size_t)ix * CIN;
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
-        if (c < J.cin) v[c] = __ldg(p + c);
-    if (J.pro.n) mp_pw_apply(J.pro, v, J.cin);
+    for (int c = 0; c < CIN; ++c) v[c] = __ldg(p + c);
+    if (J.pro.n) mp_pw_apply(J.pro, v, CIN);
 }
 
+template <int CIN, int CMID>
 __device__ __forceinline__ void mp_rotate_tile(const MPJob &J, int t)
 {
     const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
     const int x = tx * 32 + (threadIdx.x & 31);
     if (x >= J.wo) return;
-    const long long W = J.w, H = J.h;
+    const int W = J.w, H = J.h, ho = J.ho;
+    const float *src = J.src;
+    const int sp = J.src_pitch;
+    const long long cosq = J.cosq, sinq = J.sinq;
     const long long X2 = 2LL * x - W;
-    const long long cx = W << (MP_FIX_FRAC - 1), cy = H << (MP_FIX_FRAC - 1);
-    const int cmid = J.cmid;
+    const int y0 = ty * 32 + (threadIdx.x >> 5);
+    long long sx = cosq * X2 - sinq * (2LL * y0 - H) + ((long long)W << (MP_FIX_FRAC - 1));
+    long long sy = sinq * X2 + cosq * (2LL * y0 - H) + ((long long)H << (MP_FIX_FRAC - 1));
+    const long long stx = -16LL * sinq, sty = 16LL * cosq;   // y += 8
+    const bool has_pro = J.pro.n > 0;
+    const PwFast epi = mp_pw_fast(J.epi);
+    const int xo = J.flip ? (J.wo - 1 - x) : x;
+    float *dstb = J.dst;
+    const int dp = J.dst_pitch;
 #pragma unroll 1
     for (int i = 0; i < 4; ++i) {
-        const int y = ty * 32 + (threadIdx.x >> 5) + 8 * i;
-        if (y >= J.ho) break;
-        const long long Y2 = 2LL * y - H;
-        const long long sx = J.cosq * X2 - J.sinq * Y2 + cx;
-        const long long sy = J.sinq * X2 + J.cosq * Y2 + cy;
-        const int ix = (int)(sx >> MP_FIX_FRAC);
-        const int iy = (int)(sy >> MP_FIX_FRAC);
-        const float fx = (float)((int)((sx >> (MP_FIX_FRAC - 24)) & 0xFFFFFF)) * 5.9604644775390625e-8f;
-        const float fy = (float)((int)((sy >> (MP_FIX_FRAC - 24)) & 0xFFFFFF)) * 5.9604644775390625e-8f;
-        float a[4], b[4], c[4], d[4];
-        mp_load_px(J, ix, iy, a);
-        mp_load_px(J, ix + 1, iy, b);
-        mp_load_px(J, ix, iy + 1, c);
-        mp_load_px(J, ix + 1, iy + 1, d);
-        float v[4];
-        const float gx = 1.0f - fx, gy = 1.0f - fy;
+        const int y = y0 + 8 * i;
+        if (y < ho) {
+            const int ix = (int)(sx >> MP_FIX_FRAC);
+            const int iy = (int)(sy >> MP_FIX_FRAC);
+            const float fx = (float)((int)(sx >> (MP_FIX_FRAC - 24)) & 0xFFFFFF) * 5.9604644775390625e-8f;
+            const float fy = (float)((int)(sy >> (MP_FIX_FRAC - 24)) & 0xFFFFFF) * 5.9604644775390625e-8f;
+            float a[4], b[4], c[4], d[4];
+            if (!has_pro && (unsigned)ix < (unsigned)(W - 1) && (unsigned)iy < (unsigned)(H - 1)) {
+                const float *p0 = src + (iy * sp + ix * CIN);
+                const float *p1 = p0 + sp;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            v[k] = gy * (gx * a[k] + fx * b[k]) + fy * (gx * c[k] + fx * d[k]);
-        const int co = mp_pw_apply(J.epi, v, cmid);
-        const int xo = J.flip ? (J.wo - 1 - x) : x;
-        float *dst = J.dst + (size_t)y * J.dst_pitch + (size_t)xo * co;
+                for (int k = 0; k < CMID; ++k) {
+                    a[k] = __ldg(p0 + k);
+                    b[k] = __ldg(p0 + CIN + k);
+                    c[k] = __ldg(p1 + k);
+                    d[k] = __ldg(p1 + CIN + k);
+                }
+            } else {
+                mp_load_px<CIN>(J, ix, iy, a);
+                mp_load_px<CIN>(J, ix + 1, iy, b);
+                mp_load_px<CIN>(J, ix, iy + 1, c);
+                mp_load_px<CIN>(J, ix + 1, iy + 1, d);
+            }
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            const float gx = 1.0f - fx, gy = 1.0f - fy;
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (k < co) dst[k] = v[k];
+            for (int k = 0; k < CMID; ++k)
+                v[k] = gy * (gx * a[k] + fx * b[k]) + fy * (gx * c[k] + fx * d[k]);
+            float *drow = dstb + (size_t)y * dp;
+            if (epi.n == 0) {
+                float *o = drow + xo * CMID;
+#pragma unroll
+                for (int k = 0; k < CMID; ++k) o[k] = v[k];
+            } else {
+                const int co = mp_pw_apply_f(epi, J.epi, v, CMID);
+                float *o = drow + xo * co;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k < co) o[k] = v[k];
+            }
+        }
+        sx += stx;
+        sy += sty;
     }
 }
 
@@ -454,16 +510,17 @@ __device__ __forceinline__ void mp_point_tile(const MPJob &J, int t)
 }
 
 // ---------------------------------------------------------------------------
-// Kernel entry points
+// Kernel entry points.  Batch kernels read their image's job through a
+// per-tile job index (one int load), single kernels take the job by value.
 // ---------------------------------------------------------------------------
-template <int KIND>
+template <int KIND, int V>
 __device__ __forceinline__ void mp_run_tile(const MPJob &J, int lt, bool map_in_global, int *err)
 {
     extern __shared__ unsigned char mp_dyn_smem[];
     if (KIND == MPK_GAUSS) {
-        mp_gauss_tile(J, lt, mp_dyn_smem, map_in_global, err);
+        mp_gauss_tile<MPChan<V>::CIN, MPChan<V>::CMID>(J, lt, mp_dyn_smem, map_in_global, err);
     } else if (KIND == MPK_ROTATE) {
-        mp_rotate_tile(J, lt);
+        mp_rotate_tile<MPChan<V>::CIN, MPChan<V>::CMID>(J, lt);
     } else if (KIND == MPK_TRANSPOSE) {
         __shared__ float tile[32 * (32 * 4 + 1)];
         mp_transpose_tile(J, lt, tile);
@@ -472,33 +529,48 @@ __device__ __forceinline__ void mp_run_tile(const MPJob &J, int lt, bool map_in_
     }
 }
 
-template <int KIND>
-__device__ __forceinline__ void mp_batch_body(const MPJob *__restrict__ jobs, int njobs, int *err)
-{
-    const int t = blockIdx.x;
-    const int j = mp_find_job(jobs, njobs, t);
-    const MPJob &J = jobs[j];
-    const int lt = t - J.tile0;
-    if (lt >= J.ntiles) return;
-    mp_run_tile<KIND>(J, lt, true, err);
-}
-
-// One named kernel per kind and launch form, so profiles name what ran.
-#define MP_DEFINE_KERNELS(NAME, KIND)                                                        \
-    __global__ void __launch_bounds__(MP_THREADS)                                            \
-        NAME##_batch(const MPJob *__restrict__ jobs, int njobs, int *err)                    \
-    {                                                                                        \
-        mp_batch_body<KIND>(jobs, njobs, err);                                               \
-    }                                                                                        \
-    __global__ void __launch_bounds__(MP_THREADS) NAME##_single(const __grid_constant__ MPJob job, \
-                                                                int *err)                    \
-    {                                                                                        \
-        mp_run_tile<KIND>(job, blockIdx.x, false, err);                                      \
+// Named wrappers, so profiles say which kernel ran.
+#define MP_NAMED(NAME, KIND, V)                                                                    \
+    __global__ void __launch_bounds__(MP_THREADS)                                                  \
+        NAME##_batch(const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int *err)   \
+    {                                                                                              \
+        const int t = blockIdx.x;                                                                  \
+        const MPJob &J = jobs[__ldg(tile_job + t)];                                                \
+        mp_run_tile<KIND, V>(J, t - J.tile0, true, err);                                           \
+    }                                                                                              \
+    __global__ void __launch_bounds__(MP_THREADS)                                                  \
+        NAME##_single(const __grid_constant__ MPJob job, int *err)                                 \
+    {                                                                                              \
+        mp_run_tile<KIND, V>(job, blockIdx.x, false, err);                                         \
     }
-MP_DEFINE_KERNELS(mp_gauss, MPK_GAUSS)
-MP_DEFINE_KERNELS(mp_rotate, MPK_ROTATE)
-MP_DEFINE_KERNELS(mp_transpose, MPK_TRANSPOSE)
-MP_DEFINE_KERNELS(mp_point, MPK_POINT)
+MP_NAMED(mp_rotate_c1, MPK_ROTATE, 0)
+MP_NAMED(mp_rotate_c3, MPK_ROTATE, 1)
+MP_NAMED(mp_rotate_c4, MPK_ROTATE, 2)
+MP_NAMED(mp_rotate_grey3, MPK_ROTATE, 3)
+MP_NAMED(mp_rotate_grey4, MPK_ROTATE, 4)
+MP_NAMED(mp_transpose, MPK_TRANSPOSE, 0)
+MP_NAMED(mp_point, MPK_POINT, 0)
+
+// Gaussian kernels: one tile per CTA, 3 CTAs of 256 threads per SM fit in
+// registers (80 per thread).
+#define MP_GAUSS_NAMED(NAME, V)                                                                    \
+    __global__ void __launch_bounds__(MP_THREADS, 3)                                               \
+        NAME##_batch(const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int *err)   \
+    {                                                                                              \
+        const int t = blockIdx.x;                                                                  \
+        const MPJob &J = jobs[__ldg(tile_job + t)];                                                \
+        mp_run_tile<MPK_GAUSS, V>(J, t - J.tile0, true, err);                                      \
+    }                                                                                              \
+    __global__ void __launch_bounds__(MP_THREADS, 3)                                               \
+        NAME##_single(const __grid_constant__ MPJob job, int *err)                                 \
+    {                                                                                              \
+        mp_run_tile<MPK_GAUSS, V>(job, blockIdx.x, false, err);                                    \
+    }
+MP_GAUSS_NAMED(mp_gauss_c1, 0)
+MP_GAUSS_NAMED(mp_gauss_c3, 1)
+MP_GAUSS_NAMED(mp_gauss_c4, 2)
+MP_GAUSS_NAMED(mp_gauss_grey3, 3)
+MP_GAUSS_NAMED(mp_gauss_grey4, 4)
 
 // In-place channel-agnostic pointwise list (brightness, gamma) over a flat
 // float buffer: float4 body plus scalar tail.
@@ -559,67 +631,95 @@ static int mp_current_device()
     return d;
 }
 
-static const void *mp_batch_fn(int kind)
+int mp_variant(int cin, int cmid)
 {
+    if (cin == 1 && cmid == 1) return 0;
+    if (cin == 3 && cmid == 3) return 1;
+    if (cin == 4 && cmid == 4) return 2;
+    if (cin == 3 && cmid == 1) return 3;
+    if (cin == 4 && cmid == 1) return 4;
+    return -1;
+}
+
+static const void *mp_batch_fn(int kind, int v)
+{
+    static const void *gauss[5] = {(const void *)mp_gauss_c1_batch, (const void *)mp_gauss_c3_batch,
+                                   (const void *)mp_gauss_c4_batch, (const void *)mp_gauss_grey3_batch,
+                                   (const void *)mp_gauss_grey4_batch};
+    static const void *rot[5] = {(const void *)mp_rotate_c1_batch, (const void *)mp_rotate_c3_batch,
+                                 (const void *)mp_rotate_c4_batch, (const void *)mp_rotate_grey3_batch,
+                                 (const void *)mp_rotate_grey4_batch};
     switch (kind) {
-    case MPK_GAUSS: return (const void *)mp_gauss_batch;
-    case MPK_ROTATE: return (const void *)mp_rotate_batch;
+    case MPK_GAUSS: return (v >= 0 && v < 5) ? gauss[v] : nullptr;
+    case MPK_ROTATE: return (v >= 0 && v < 5) ? rot[v] : nullptr;
     case MPK_TRANSPOSE: return (const void *)mp_transpose_batch;
     default: return (const void *)mp_point_batch;
     }
 }
 
-MPStatus mp_prepare_kind(int kind, size_t smem)
+static const void *mp_single_fn(int kind, int v)
 {
-    return mp_prepare_smem(mp_batch_fn(kind), smem);
+    static const void *gauss[5] = {(const void *)mp_gauss_c1_single, (const void *)mp_gauss_c3_single,
+                                   (const void *)mp_gauss_c4_single, (const void *)mp_gauss_grey3_single,
+                                   (const void *)mp_gauss_grey4_single};
+    static const void *rot[5] = {(const void *)mp_rotate_c1_single, (const void *)mp_rotate_c3_single,
+                                 (const void *)mp_rotate_c4_single, (const void *)mp_rotate_grey3_single,
+                                 (const void *)mp_rotate_grey4_single};
+    switch (kind) {
+    case MPK_GAUSS: return (v >= 0 && v < 5) ? gauss[v] : nullptr;
+    case MPK_ROTATE: return (v >= 0 && v < 5) ? rot[v] : nullptr;
+    case MPK_TRANSPOSE: return (const void *)mp_transpose_single;
+    default: return (const void *)mp_point_single;
+    }
+}
+
+MPStatus mp_prepare_kind(int kind, int variant, size_t smem)
+{
+    const void *fn = mp_batch_fn(kind, variant);
+    if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
+    MPStatus st = mp_prepare_smem(fn, smem);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    return MILLIPYDE_SUCCESS;
 }
 
 // Kernel launch only (no allocation, no attribute change), so it may be
-// captured into a CUDA graph; mp_prepare_kind must have run for (kind, smem).
-MPStatus mp_launch_kind(int kind, const MPJob *jobs_dev, int njobs, int total_tiles,
-                        size_t smem, int *err, cudaStream_t s)
+// captured into a CUDA graph; mp_prepare_kind must have run for the launch.
+// `gauss` carries the tile geometry of GAUSS launches.
+MPStatus mp_launch_kind(int kind, int variant, const MPJob *jobs_dev, const int *tile_job,
+                        int total_tiles, size_t smem, int *err, cudaStream_t s, const int *gauss)
 {
-    if (total_tiles <= 0 || njobs <= 0) return MILLIPYDE_SUCCESS;
-    const void *fn = mp_batch_fn(kind);
-    void *args[] = {(void *)&jobs_dev, (void *)&njobs, (void *)&err};
+    if (total_tiles <= 0) return MILLIPYDE_SUCCESS;
+    const void *fn = mp_batch_fn(kind, variant);
+    if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
+    (void)gauss;
+    void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&err};
     return mp_cuda_status(
         cudaLaunchKernel(fn, dim3(total_tiles), dim3(MP_THREADS), args, smem, s));
 }
 
-MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem, cudaStream_t s)
+static MPStatus mp_launch_single_impl(int kind, const MPJob &job, size_t smem, int *err, cudaStream_t s)
 {
     if (job.ntiles <= 0) return MILLIPYDE_SUCCESS;
-    int *err = mp_device_error_word(mp_current_device());
-    const void *fn;
-    switch (kind) {
-    case MPK_GAUSS: fn = (const void *)mp_gauss_single; break;
-    case MPK_ROTATE: fn = (const void *)mp_rotate_single; break;
-    case MPK_TRANSPOSE: fn = (const void *)mp_transpose_single; break;
-    default: fn = (const void *)mp_point_single; break;
-    }
+    const void *fn = mp_single_fn(kind, mp_variant(job.cin, job.cmid));
+    if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
     MPStatus st = mp_prepare_smem(fn, smem);
     if (st != MILLIPYDE_SUCCESS) return st;
     void *args[] = {(void *)&job, (void *)&err};
-    return mp_cuda_status(
-        cudaLaunchKernel(fn, dim3(job.ntiles), dim3(MP_THREADS), args, smem, s));
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(job.ntiles), dim3(MP_THREADS), args, smem, s));
+}
+
+MPStatus mp_launch_single(int kind, const MPJob &job, size_t smem, cudaStream_t s)
+{
+    int *err = mp_device_error_word(mp_current_device());
+    if (!err) return MP_ERROR_NO_DEVICE;
+    return mp_launch_single_impl(kind, job, smem, err, s);
 }
 
 // Single-job launch reporting into a caller-supplied device error word
 // (allocation-free path: nothing here allocates device memory).
 MPStatus mp_launch_single_err(int kind, const MPJob &job, size_t smem, int *err, cudaStream_t s)
 {
-    if (job.ntiles <= 0) return MILLIPYDE_SUCCESS;
-    const void *fn;
-    switch (kind) {
-    case MPK_GAUSS: fn = (const void *)mp_gauss_single; break;
-    case MPK_ROTATE: fn = (const void *)mp_rotate_single; break;
-    case MPK_TRANSPOSE: fn = (const void *)mp_transpose_single; break;
-    default: fn = (const void *)mp_point_single; break;
-    }
-    MPStatus st = mp_prepare_smem(fn, smem);
-    if (st != MILLIPYDE_SUCCESS) return st;
-    void *args[] = {(void *)&job, (void *)&err};
-    return mp_cuda_status(cudaLaunchKernel(fn, dim3(job.ntiles), dim3(MP_THREADS), args, smem, s));
+    return mp_launch_single_impl(kind, job, smem, err, s);
 }
 
 MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s)

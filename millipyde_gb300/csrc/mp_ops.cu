@@ -211,17 +211,42 @@ static int mp_max_smem_optin()
 
 // Tile (tw, th) for a GAUSS launch: the largest candidate whose shared memory
 // lets two CTAs share an SM, else the largest that fits at all.
+// Autotuned gaussian tiles, set by mpk_tune_set_gauss_tile (the Python
+// autotuner times candidate tiles on the device and records the fastest).
+struct MPTuneEntry {
+    int cin, cmid, has_pro, rlo, rhi, tw, th;
+};
+static std::vector<MPTuneEntry> mp_tune_table;
+static std::mutex mp_tune_mutex;
+
+static bool mp_gauss_tile_fits(int tw, int th, int r, int cin, int cmid, int has_pro)
+{
+    return tw >= 8 && th >= 8 && tw % 8 == 0 && th % 8 == 0 && th + 2 * r <= 256 &&
+           mp_gauss_smem_bytes(tw, th, r, cin, cmid, has_pro) <= (size_t)mp_max_smem_optin();
+}
+
 static void mp_gauss_tiles(int r, int cin, int cmid, int has_pro, int *tw, int *th)
 {
-    static const int grey[][2] = {{128, 32}, {64, 32}, {64, 16}, {32, 16}, {32, 8}, {16, 8}, {8, 8}};
+    {
+        std::lock_guard<std::mutex> lk(mp_tune_mutex);
+        for (const MPTuneEntry &e : mp_tune_table)
+            if (e.cin == cin && e.cmid == cmid && e.has_pro == (has_pro ? 1 : 0) && r >= e.rlo &&
+                r <= e.rhi && mp_gauss_tile_fits(e.tw, e.th, r, cin, cmid, has_pro)) {
+                *tw = e.tw;
+                *th = e.th;
+                return;
+            }
+    }
+    static const int grey[][2] = {{64, 64}, {128, 32}, {64, 32}, {64, 16}, {32, 16}, {16, 8}, {8, 8}};
     static const int colr[][2] = {{64, 32}, {32, 32}, {32, 16}, {16, 16}, {16, 8}, {8, 8}};
     const int(*cand)[2] = cmid == 1 ? grey : colr;
     const int nc = cmid == 1 ? 7 : 6;
     const size_t lim = (size_t)mp_max_smem_optin();
-    for (int pass = 0; pass < 2; ++pass) {
-        const size_t budget = pass == 0 ? lim / 2 - 1024 : lim;
+    for (int pass = 0; pass < 3; ++pass) {
+        // prefer tiles that let 3 CTAs (the register limit) share an SM
+        const size_t budget = pass == 0 ? lim / 3 - 1024 : pass == 1 ? lim / 2 - 1024 : lim;
         for (int i = 0; i < nc; ++i) {
-            if (cand[i][1] + 2 * r > 256) continue;
+            if (cand[i][1] + 2 * r > 256) continue;   // TMA box height limit
             if (mp_gauss_smem_bytes(cand[i][0], cand[i][1], r, cin, cmid, has_pro) <= budget) {
                 *tw = cand[i][0];
                 *th = cand[i][1];
@@ -341,20 +366,93 @@ static MPStatus mp_run_segment_single(const Seg &sg, const MPImage &in, const MP
 // ---------------------------------------------------------------------------
 struct MPLaunch {
     int kind;
-    size_t job_off;
+    int variant;      // channel specialisation of GAUSS / ROTATE launches
+    size_t job_off;   // first job of this launch in the job table
+    size_t tile_off;  // first entry of this launch in the tile -> job map
     int njobs;
     int total_tiles;
     size_t smem;
     double bytes;   // algorithmic bytes: inputs read once + outputs written once
+    int gauss[4];   // GAUSS: tile width, tile height, largest radius, all sources TMA-able
 };
 
 struct MPPlanImpl {
     std::vector<MPLaunch> launches;
+    void *tables = nullptr;    // one device block: job table, then tile -> job map
     MPJob *jobs_dev = nullptr;
+    int *tiles_dev = nullptr;
     void *scratch = nullptr;
     int *err = nullptr;        // device error word the kernels report into
     int device = 0;
     cudaStream_t stream = nullptr;
+};
+
+// Kernel variant of a segment (channel specialisation for GAUSS / ROTATE).
+static int mp_seg_variant(const Seg &sg)
+{
+    return (sg.kind == MPK_GAUSS || sg.kind == MPK_ROTATE) ? mp_variant(sg.cin, sg.cmid) : 0;
+}
+
+static int mp_seg_key(const Seg &sg) { return sg.kind * 16 + mp_seg_variant(sg); }
+
+// Host-side job table and tile -> job map of a plan under construction.
+struct MPTables {
+    std::vector<MPJob> jobs;
+    std::vector<int> tiles;
+
+    // Appends one launch made of the jobs in js (jobs with no tiles dropped).
+    MPStatus add(std::vector<MPLaunch> &launches, int kind, int variant, size_t smem,
+                 std::vector<MPJob> &js, double bytes)
+    {
+        MPLaunch L;
+        L.kind = kind;
+        L.variant = variant;
+        L.job_off = jobs.size();
+        L.tile_off = tiles.size();
+        L.njobs = 0;
+        L.total_tiles = 0;
+        L.smem = smem;
+        L.bytes = bytes;
+        L.gauss[0] = L.gauss[1] = L.gauss[2] = 0;
+        L.gauss[3] = 1;
+        for (MPJob &J : js) {
+            if (J.ntiles <= 0) continue;
+            if ((long long)L.total_tiles + J.ntiles > 0x7fffffffLL) return MP_ERROR_TOO_LARGE;
+            J.tile0 = L.total_tiles;
+            L.total_tiles += J.ntiles;
+            tiles.insert(tiles.end(), (size_t)J.ntiles, L.njobs);
+            if (kind == MPK_GAUSS) {
+                L.gauss[0] = J.tw;
+                L.gauss[1] = J.th;
+                L.gauss[2] = std::max(L.gauss[2], J.radius);
+                L.gauss[3] &= J.use_tma;
+            }
+            jobs.push_back(J);
+            L.njobs++;
+        }
+        if (L.njobs == 0) return MILLIPYDE_SUCCESS;
+        if (kind < MPK_POINT_ADJ) {
+            MPStatus e = mp_prepare_kind(kind, variant, smem);
+            if (e != MILLIPYDE_SUCCESS) return e;
+        }
+        launches.push_back(L);
+        return MILLIPYDE_SUCCESS;
+    }
+
+    // One device block: jobs (128-byte aligned entries), then the tile map.
+    MPStatus upload(MPPlanImpl *P, cudaStream_t s)
+    {
+        if (jobs.empty()) return MILLIPYDE_SUCCESS;
+        const size_t jb = jobs.size() * sizeof(MPJob), tb = tiles.size() * sizeof(int);
+        std::vector<unsigned char> host(jb + tb);
+        memcpy(host.data(), jobs.data(), jb);
+        memcpy(host.data() + jb, tiles.data(), tb);
+        MPStatus st = mp_malloc_async(&P->tables, jb + tb, s);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        P->jobs_dev = (MPJob *)P->tables;
+        P->tiles_dev = (int *)((unsigned char *)P->tables + jb);
+        return mp_cuda_status(cudaMemcpyAsync(P->tables, host.data(), jb + tb, cudaMemcpyHostToDevice, s));
+    }
 };
 
 static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage *in,
@@ -403,7 +501,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
         const auto &A = segs[a], &B = segs[b];
         if (A.size() != B.size()) return A.size() < B.size();
         for (size_t k = 0; k < A.size(); ++k)
-            if (A[k].kind != B[k].kind) return A[k].kind < B[k].kind;
+            if (mp_seg_key(A[k]) != mp_seg_key(B[k])) return mp_seg_key(A[k]) < mp_seg_key(B[k]);
         return a < b;
     };
     std::sort(order.begin(), order.end(), sig_less);
@@ -420,7 +518,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             while (i < order.size()) {
                 const auto &sg = segs[order[i]];
                 bool same = sg.size() == sig0.size();
-                for (size_t k = 0; same && k < sg.size(); ++k) same = sg[k].kind == sig0[k].kind;
+                for (size_t k = 0; same && k < sg.size(); ++k) same = mp_seg_key(sg[k]) == mp_seg_key(sig0[k]);
                 if (!same) break;
                 size_t b = 0;
                 for (size_t k = 0; k + 1 < sg.size(); ++k)
@@ -438,7 +536,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
     MPStatus st = mp_malloc_async(&P->scratch, scratch_need, s);
     if (st != MILLIPYDE_SUCCESS) return st;
     // 4. jobs
-    std::vector<MPJob> jobs;
+    MPTables T;
     for (const Chunk &ch : chunks) {
         const size_t nseg = segs[ch.imgs[0]].size();
         // intermediate images of this chunk
@@ -474,13 +572,8 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 mp_gauss_tiles(rmax, cinm, cmidm, pro, &tw, &th);
                 smem = mp_gauss_smem_bytes(tw, th, rmax, cinm, cmidm, pro);
             }
-            MPLaunch L;
-            L.kind = kind;
-            L.job_off = jobs.size();
-            L.njobs = 0;
-            L.total_tiles = 0;
-            L.smem = smem;
-            L.bytes = 0.0;
+            std::vector<MPJob> js;
+            double bytes = 0.0;
             for (size_t q = 0; q < ch.imgs.size(); ++q) {
                 const int img = ch.imgs[q];
                 const Seg &sg = segs[img][k];
@@ -489,39 +582,26 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 MPJob J;
                 st = mp_fill_job(J, sg, src, dst, tw, th);
                 if (st != MILLIPYDE_SUCCESS) return st;
-                if (J.ntiles <= 0) continue;
-                if ((long long)L.total_tiles + J.ntiles > 0x7fffffffLL) return MP_ERROR_TOO_LARGE;
-                J.tile0 = L.total_tiles;
-                L.total_tiles += J.ntiles;
-                L.bytes += 4.0 * ((double)src.height * src.width * src.channels +
-                                  (double)dst.height * dst.width * dst.channels);
-                jobs.push_back(J);
-                L.njobs++;
+                bytes += 4.0 * ((double)src.height * src.width * src.channels +
+                                (double)dst.height * dst.width * dst.channels);
+                js.push_back(J);
             }
-            if (L.njobs > 0) {
-                st = mp_prepare_kind(L.kind, L.smem);
-                if (st != MILLIPYDE_SUCCESS) return st;
-                P->launches.push_back(L);
-            }
+            st = T.add(P->launches, kind, mp_seg_variant(segs[ch.imgs[0]][k]), smem, js, bytes);
+            if (st != MILLIPYDE_SUCCESS) return st;
         }
     }
-    if (!jobs.empty()) {
-        st = mp_malloc_async((void **)&P->jobs_dev, jobs.size() * sizeof(MPJob), s);
-        if (st != MILLIPYDE_SUCCESS) return st;
-        MP_CUDA_TRY(cudaMemcpyAsync(P->jobs_dev, jobs.data(), jobs.size() * sizeof(MPJob),
-                                    cudaMemcpyHostToDevice, s));
-    }
-    return MILLIPYDE_SUCCESS;
+    return T.upload(P, s);
 }
 
 static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
 {
     for (const MPLaunch &L : P->launches) {
         MPStatus st = L.kind >= MPK_POINT_ADJ
-                          ? mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles,
-                                              P->err, s)
-                          : mp_launch_kind(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles,
-                                           L.smem, P->err, s);
+                          ? mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off,
+                                              L.total_tiles, P->err, s)
+                          : mp_launch_kind(L.kind, L.variant, P->jobs_dev + L.job_off,
+                                           P->tiles_dev + L.tile_off, L.total_tiles, L.smem, P->err, s,
+                                           L.gauss);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -529,9 +609,11 @@ static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
 
 static void mp_plan_free(MPPlanImpl *P, cudaStream_t s)
 {
-    mp_free_async(P->jobs_dev, s);
+    mp_free_async(P->tables, s);
     mp_free_async(P->scratch, s);
+    P->tables = nullptr;
     P->jobs_dev = nullptr;
+    P->tiles_dev = nullptr;
     P->scratch = nullptr;
 }
 
@@ -574,8 +656,12 @@ MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream)
     if (first < 0 || count < 0 || first + count > (int)P->launches.size()) return MP_ERROR_INVALID_ARGS;
     for (int i = first; i < first + count; ++i) {
         const MPLaunch &L = P->launches[i];
-        MPStatus st = mp_launch_kind(L.kind, P->jobs_dev + L.job_off, L.njobs, L.total_tiles, L.smem,
-                                     P->err, (cudaStream_t)stream);
+        MPStatus st = L.kind >= MPK_POINT_ADJ
+                          ? mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off,
+                                              L.total_tiles, P->err, (cudaStream_t)stream)
+                          : mp_launch_kind(L.kind, L.variant, P->jobs_dev + L.job_off,
+                                           P->tiles_dev + L.tile_off, L.total_tiles, L.smem, P->err,
+                                           (cudaStream_t)stream, L.gauss);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -754,6 +840,7 @@ static MPStatus mp_obj_apply(MPObjData *o, int op, double p0, double p1, double 
 {
     MPImage in;
     MPStatus st = mp_obj_image(o, &in);
+    if (st == MP_ERROR_UNSUPPORTED_TYPE) return mp_legacy_apply(o, op, p0, p1, p2);
     if (st != MILLIPYDE_SUCCESS) return st;
     ROp r;
     r.op = op;
@@ -1296,29 +1383,11 @@ extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *p
         P.device = dev;
         P.stream = s;
         P.err = err;
-        std::vector<MPJob> jobs;
+        MPTables T;
         auto add_launch = [&](int kind, size_t smem, std::vector<MPJob> &js) -> MPStatus {
-            MPLaunch L;
-            L.kind = kind;
-            L.job_off = jobs.size();
-            L.njobs = 0;
-            L.total_tiles = 0;
-            L.smem = smem;
-            L.bytes = 0;
-            for (MPJob &J : js) {
-                if (J.ntiles <= 0) continue;
-                J.tile0 = L.total_tiles;
-                L.total_tiles += J.ntiles;
-                jobs.push_back(J);
-                L.njobs++;
-            }
-            if (L.njobs == 0) return MILLIPYDE_SUCCESS;
-            if (kind < MPK_POINT_ADJ) {
-                MPStatus e = mp_prepare_kind(kind, smem);
-                if (e != MILLIPYDE_SUCCESS) return e;
-            }
-            P.launches.push_back(L);
-            return MILLIPYDE_SUCCESS;
+            int v = 0;
+            if ((kind == MPK_GAUSS || kind == MPK_ROTATE) && !js.empty()) v = mp_variant(js[0].cin, js[0].cmid);
+            return T.add(P.launches, kind, v, smem, js, 0.0);
         };
         // one-op segment for op k of image q
         auto seg_of = [&](int q, int k) -> Seg {
@@ -1466,15 +1535,9 @@ extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *p
             cur = nxt;
             k = j - 1;
         }
-        if (st == MILLIPYDE_SUCCESS && !jobs.empty()) {
-            st = mp_malloc_async((void **)&P.jobs_dev, jobs.size() * sizeof(MPJob), s);
-            if (st == MILLIPYDE_SUCCESS)
-                st = mp_cuda_status(cudaMemcpyAsync(P.jobs_dev, jobs.data(), jobs.size() * sizeof(MPJob),
-                                                    cudaMemcpyHostToDevice, s));
-        }
+        if (st == MILLIPYDE_SUCCESS) st = T.upload(&P, s);
         if (st == MILLIPYDE_SUCCESS) st = mp_plan_launch(&P, s);
-        mp_free_async(P.jobs_dev, s);
-        P.jobs_dev = nullptr;
+        mp_plan_free(&P, s);
     }
     mp_free_async(scratch, s);
     return st;
@@ -1529,4 +1592,40 @@ MPStatus mp_run_image_noalloc(const MPStage *stages, int nstages, uint64_t seed,
         cur = dst;
     }
     return MILLIPYDE_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuning hooks
+// ---------------------------------------------------------------------------
+extern "C" MPStatus mpk_tune_set_gauss_tile(int cin, int cmid, int has_pro, int radius_lo,
+                                            int radius_hi, int tw, int th)
+{
+    if (mp_variant(cin, cmid) < 0 || radius_lo < 1 || radius_hi < radius_lo ||
+        radius_hi > MP_MAX_RADIUS)
+        return MP_ERROR_INVALID_ARGS;
+    if (!mp_gauss_tile_fits(tw, th, radius_hi, cin, cmid, has_pro)) return MP_ERROR_TOO_LARGE;
+    std::lock_guard<std::mutex> lk(mp_tune_mutex);
+    MPTuneEntry e = {cin, cmid, has_pro ? 1 : 0, radius_lo, radius_hi, tw, th};
+    for (MPTuneEntry &x : mp_tune_table)
+        if (x.cin == cin && x.cmid == cmid && x.has_pro == e.has_pro && x.rlo == radius_lo &&
+            x.rhi == radius_hi) {
+            x = e;
+            return MILLIPYDE_SUCCESS;
+        }
+    mp_tune_table.insert(mp_tune_table.begin(), e);
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_tune_get_gauss_tile(int cin, int cmid, int has_pro, int radius, int *tw, int *th)
+{
+    if (mp_variant(cin, cmid) < 0 || radius < 1 || radius > MP_MAX_RADIUS || !tw || !th)
+        return MP_ERROR_INVALID_ARGS;
+    mp_gauss_tiles(radius, cin, cmid, has_pro, tw, th);
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" void mpk_tune_clear(void)
+{
+    std::lock_guard<std::mutex> lk(mp_tune_mutex);
+    mp_tune_table.clear();
 }

@@ -35,6 +35,7 @@ MPStatus mp_cuda_status(cudaError_t e)
 {
     if (e == cudaSuccess) return MILLIPYDE_SUCCESS;
     mp_set_cuda_error(e);
+    cudaGetLastError();   // clear a non-sticky error so the next call does not report it
     if (e == cudaErrorMemoryAllocation) return MP_ERROR_OUT_OF_MEMORY;
     if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return MP_ERROR_NO_DEVICE;
     return MP_ERROR_CUDA;
@@ -224,6 +225,17 @@ MPStatus mp_check_device_error(cudaStream_t stream)
         cudaMemsetAsync(w, 0, sizeof(int), stream);
         return MP_ERROR_KERNEL_TIMEOUT;
     }
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpdev_get_device_name(int device_id, char *buf, int len)
+{
+    if (!buf || len <= 0) return MP_ERROR_INVALID_ARGS;
+    buf[0] = 0;
+    if (!mpdev_is_valid_device(device_id)) return MP_ERROR_NO_DEVICE;
+    cudaDeviceProp prop;
+    MP_CUDA_TRY(cudaGetDeviceProperties(&prop, device_id));
+    snprintf(buf, (size_t)len, "%s", prop.name);
     return MILLIPYDE_SUCCESS;
 }
 
