@@ -255,7 +255,9 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     tpp = ncu_traffic_per_px(dom)
     traffic = tpp * dk["px"] / dk["launches"] if tpp else None
-    kind_names = {0: "pointwise", 1: "gaussian(+rgb2grey prologue)", 2: "rotate(+gamma epilogue)", 3: "transpose"}
+    kind_names = {0: "pointwise", 1: "gaussian tiles", 2: "rotate tiles", 3: "transpose",
+                  4: "gaussian strip stream", 5: "rotate footprint (gamma epilogue)",
+                  8: "gaussian 1-channel stream (rgb2grey prologue)"}
 
     per_op = e2e = cpu_v = None
     po_steps = e2e_steps = 0

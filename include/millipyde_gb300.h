@@ -311,7 +311,8 @@ int mpk_plan_num_launches(const MPPlan *plan);
 MPStatus mpk_plan_destroy(MPPlan *plan);
 
 /* Launches launches [first, first+count) of a plan only, and describes
- * launch i (kind: 0 pointwise, 1 gaussian, 2 rotate, 3 transpose; njobs
+ * launch i (kind: 0 pointwise, 1 gaussian, 2 rotate, 3 transpose,
+ * 4 streaming gaussian, 5 footprint-staged rotate; njobs
  * images; tiles CTAs; bytes = algorithmic bytes moved: every input pixel read
  * once and every output pixel written once, float32). */
 MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream);
@@ -338,6 +339,9 @@ MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, const MPImage
 MPStatus mpk_tune_set_gauss_tile(int cin, int cmid, int has_pro, int radius_lo, int radius_hi,
                                  int tw, int th);
 MPStatus mpk_tune_get_gauss_tile(int cin, int cmid, int has_pro, int radius, int *tw, int *th);
+/* TMA stage count (2..6) of the streaming gaussian for a channel count
+ * after the prologue (1, 3 or 4). */
+MPStatus mpk_tune_set_stream(int cmid, int stages);
 void mpk_tune_clear(void);
 
 /* Differentiable chains on dense batches (the autograd path): B images of

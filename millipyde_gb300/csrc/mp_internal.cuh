@@ -20,8 +20,82 @@
 #define MP_SPIN_FAST 2048                 // try_wait polls before backing off
 #define MP_SPIN_LIMIT (1u << 21)          // bounded wait: ~2 s with 1 us backoff
 
-// Segment kernel kinds.
-enum MPKind { MPK_POINT = 0, MPK_GAUSS = 1, MPK_ROTATE = 2, MPK_TRANSPOSE = 3 };
+// Segment kernel kinds.  GSTREAM is the strip-streaming gaussian
+// (mp_stream.cu), used for GAUSS segments whose source rows are TMA-legal and
+// whose epilogue is per-channel.
+// RSTREAM is the footprint-staged rotate (mp_rot.cu), used for ROTATE
+// segments without a prologue whose source rows are TMA-legal.
+// VH is the single-channel streaming gaussian (mp_vh.cuh), for radii up to
+// MP_VH_RMAX.
+enum MPKind {
+    MPK_POINT = 0, MPK_GAUSS = 1, MPK_ROTATE = 2, MPK_TRANSPOSE = 3, MPK_GSTREAM = 4, MPK_RSTREAM = 5,
+    MPK_VH = 8
+};
+#define MP_VH_RMAX 12
+
+
+// Output tile of the footprint-staged rotate per channel count.
+__host__ __device__ constexpr int mp_ro_tw(int c) { return c == 1 ? 64 : 32; }
+__host__ __device__ constexpr int mp_ro_th(int c) { return 32; }
+#define MP_RO_NT 256
+
+// ---------------------------------------------------------------------------
+// Streaming gaussian geometry (host and device agree on it).  Rows are
+// processed in blocks of MP_GS_RB; sizes in floats unless noted.  The strip
+// width and CTA size are fixed per channel count after the prologue (cmid),
+// and radii are rounded up to a compiled bucket (exact up to 12, then 16 and
+// 24; larger radii run a loop over the taps).
+// ---------------------------------------------------------------------------
+#define MP_GS_MAXNS 6
+
+// strip width, rows per block and CTA size per channel count after the prologue
+__host__ __device__ constexpr int mp_gs_sw(int cmid) { return 64; }
+__host__ __device__ constexpr int mp_gs_rb(int cmid) { return cmid == 1 ? 16 : 8; }
+__host__ __device__ constexpr int mp_gs_nt(int cmid) { return cmid == 1 ? 128 : 64 * cmid; }
+__host__ __device__ constexpr int mp_gs_bucket(int r) { return r <= 12 ? r : (r <= 16 ? 16 : (r <= 24 ? 24 : r)); }
+
+struct GsGeom {
+    int SW, lgSW;     // strip width in output pixels (power of two)
+    int NS;           // TMA stages in the ring
+    int BOXW;         // floats per TMA box row (48 for 3 source channels, else 64)
+    int BOXS;         // floats from one box of a stage to the next
+    int STG;          // floats per stage
+    int GW;           // row stride of the channel planes G
+    int HW;           // row stride of the horizontal-pass ring H (SW + 4)
+    int HR;           // rows of H per channel (ring + mirrored head + read-ahead)
+    int offS, offG, offH;   // byte offsets from the 128-byte aligned base
+    int total;              // bytes (without alignment slack)
+};
+
+__host__ __device__ __forceinline__ int mp_gs_boxw(int cin) { return cin == 3 ? 48 : 64; }
+
+// Geometry for ns stages and largest bucket radius rb over the launch.
+// Radii outside the compiled buckets run loop passes that read up to 8 rows
+// past the vertical window, so the H ring always carries 8 spare rows.
+__host__ __device__ __forceinline__ GsGeom mp_gs_geom(int ns, int rb, int cin, int cmid)
+{
+    GsGeom g;
+    const int sw = mp_gs_sw(cmid), RB = mp_gs_rb(cmid);
+    g.SW = sw;
+    g.lgSW = 0;
+    while ((1 << g.lgSW) < sw) ++g.lgSW;
+    g.NS = ns;
+    g.BOXW = mp_gs_boxw(cin);
+    const int R4 = (rb + 3) & ~3;
+    const int GL = (sw + 2 * R4 + 4 + 15) & ~15;           // pixels per G row
+    const int nbx = (GL * cin + g.BOXW - 1) / g.BOXW;
+    g.BOXS = g.BOXW * RB + 32;                             // +128 B: box starts stay 128-B aligned
+    g.STG = nbx * g.BOXS;
+    g.GW = ((GL + 31) & ~31) + 4;                          // = 4 (mod 32): conflict-free column reads
+    g.HW = sw + 4;
+    const int L = (2 * rb + RB - 1) / RB;
+    g.HR = (L + 1) * RB + 2 * rb + 8;
+    g.offS = 1152;                                         // barriers + two 128-float tap arrays
+    g.offG = g.offS + ns * g.STG * 4;
+    g.offH = g.offG + cmid * RB * g.GW * 4;
+    g.total = g.offH + cmid * g.HR * g.HW * 4;
+    return g;
+}
 
 // Device-side error word values (written by kernels, read by the host).
 enum { MP_KERR_NONE = 0, MP_KERR_TIMEOUT = 1 };
@@ -66,6 +140,8 @@ struct MPJob {
     int pw_slot[MP_MAX_PW];    // POINT adjoint: acc slot (x3) of each pointwise op
     float cth, sth;            // ROTATE adjoint: cos/sin of the angle
     float wts_h[MP_MAX_TAPS];  // GAUSS: horizontal taps when hsep
+    int vec_out;               // GSTREAM: destination rows 16-byte aligned (vector stores)
+    int bxw, byh;              // RSTREAM: footprint box (floats per row, rows)
 };
 
 // ---------------------------------------------------------------------------
@@ -143,6 +219,30 @@ __device__ __forceinline__ int mp_pw_apply_f(const PwFast &f, const PwList &L, f
     if (f.n == 0) return c;
     if (f.n == 1) return mp_pw_op(f.op, f.p0, f.p1, f.p2, v, c);
     return mp_pw_apply(L, v, c);
+}
+
+// One channel-preserving pointwise op on a single value of channel c of a
+// cm-channel pixel: the same arithmetic as mp_pw_op, one channel at a time
+// (rgb2grey mixes channels and is never applied this way).
+__device__ __forceinline__ float mp_pw_chan(int op, float p0, float p1, float p2, float v, int c, int cm)
+{
+    const bool colour = !(cm == 4 && c == 3);
+    switch (op) {
+    case MP_OP_BRIGHTNESS: return colour ? mp_clamp01(v + p0) : v;
+    case MP_OP_ADJUST_GAMMA: return colour ? mp_clamp01(p1 * __powf(v, p0)) : v;
+    case MP_OP_COLORIZE:
+        if (cm >= 3 && c < 3) return fminf(1.0f, v * (c == 0 ? p0 : (c == 1 ? p1 : p2)));
+        return v;
+    default: return v;
+    }
+}
+
+__device__ __forceinline__ float mp_pw_chan_f(const PwFast &f, const PwList &L, float v, int c, int cm)
+{
+    if (f.n == 0) return v;
+    if (f.n == 1) return mp_pw_chan(f.op, f.p0, f.p1, f.p2, v, c, cm);
+    for (int i = 0; i < L.n; ++i) v = mp_pw_chan(L.op[i].op, L.op[i].p0, L.op[i].p1, L.op[i].p2, v, c, cm);
+    return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -278,4 +378,29 @@ MPStatus mp_legacy_apply(MPObjData *o, int op, double p0, double p1, double p2);
 MPStatus mp_launch_flat(float *data, size_t n, const PwList &L, cudaStream_t s);
 // Dynamic shared memory a GAUSS launch needs for the given geometry.
 size_t mp_gauss_smem_bytes(int tw, int th, int radius, int cin, int cmid, int has_pro);
+// Footprint-staged rotate (mp_rot.cu): `buf_floats` = floats of one
+// footprint buffer (the largest box of the launch, 128-byte multiple).
+MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm);
+MPStatus mp_ro_launch(int c, const MPJob *jobs_dev, const int *tile_job, int total, int buf_floats, int grid,
+                      int *err, cudaStream_t s);
+MPStatus mp_ro_launch_single(int c, const MPJob &job, int buf_floats, int grid, int *err, cudaStream_t s);
+size_t mp_ro_smem(int buf_floats);
+// Single-channel streaming gaussian (mp_vh*.cu): strip width in output
+// pixels for a radius, resident CTAs per SM, launches.
+int mp_vh_strip(int radius);
+int mp_vh_fit_strip(int radius, int w);
+MPStatus mp_vh_prepare(int cin, int *ctas_per_sm);
+MPStatus mp_vh_launch(int cin, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
+                      cudaStream_t s);
+MPStatus mp_vh_launch_single(int cin, const MPJob &job, int grid, int *err, cudaStream_t s);
+
+// Streaming gaussian (mp_stream.cu).  mp_gs_prepare raises the
+// shared-memory limit and returns the resident CTAs per SM (call outside
+// capture); mp_gs_launch runs `grid` persistent CTAs over `total` strip
+// items of a job table.
+MPStatus mp_gs_prepare(int variant, size_t smem, int *ctas_per_sm);
+MPStatus mp_gs_launch(int variant, const MPJob *jobs_dev, const int *tile_job, int total, const GsGeom &g,
+                      int grid, int *err, cudaStream_t s);
+MPStatus mp_gs_launch_single(int variant, const MPJob &job, const GsGeom &g, int grid, int *err,
+                             cudaStream_t s);
 #endif

@@ -333,6 +333,183 @@ static MPStatus mp_fill_job(MPJob &J, const Seg &sg, const MPImage &in, const MP
     return MILLIPYDE_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Streaming gaussian (mp_stream.cu) selection.
+// ---------------------------------------------------------------------------
+struct MPStreamTune {
+    int cmid, ns;
+};
+static std::vector<MPStreamTune> mp_stream_tune;   // guarded by mp_tune_mutex
+
+static int mp_num_sms()
+{
+    static int n = 0;
+    if (!n) {
+        int d = 0;
+        cudaGetDevice(&d);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 1;
+        }
+    }
+    return n;
+}
+
+// A GAUSS segment runs on the streaming kernel when its source rows are
+// TMA-legal (16-byte aligned base and pitch) and its epilogue keeps the
+// channel count (no rgb2grey after the blur).
+static bool mp_stream_ok(const Seg &sg, const MPImage &in)
+{
+    if (sg.kind != MPK_GAUSS || mp_variant(sg.cin, sg.cmid) < 0 || sg.cout != sg.cmid) return false;
+    for (int i = 0; i < sg.epi.n; ++i)
+        if (sg.epi.op[i].op == MP_OP_RGB2GREY) return false;
+    if ((in.pitch % 16) || ((uintptr_t)in.data % 16) || in.width <= 0 || in.height <= 0) return false;
+    return mp_get_encode_tiled() != nullptr;
+}
+
+// TMA stage count of the streaming gaussian for a channel count.
+static int mp_stream_stages(int cmid)
+{
+    int ns = cmid == 1 ? 2 : 3;
+    std::lock_guard<std::mutex> lk(mp_tune_mutex);
+    for (const MPStreamTune &t : mp_stream_tune)
+        if (t.cmid == cmid) ns = t.ns;
+    return ns;
+}
+
+// Rows per strip item: about three items per resident CTA over the launch,
+// at least 128 rows so the 2r halo rows stay a small share.
+static int mp_stream_rows(long long strip_rows, int grid)
+{
+    const long long target = 3LL * (grid > 0 ? grid : 1);
+    long long rs = (strip_rows + target - 1) / target;
+    if (rs < 128) rs = 128;
+    rs = (rs + 15) / 16 * 16;   // a multiple of every block height
+    if (rs > (1 << 20)) rs = 1 << 20;
+    return (int)rs;
+}
+
+static MPStatus mp_fill_job_stream(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out,
+                                   int sw, int rs)
+{
+    memset(&J, 0, sizeof(J));
+    J.src = (const float *)in.data;
+    J.dst = (float *)out.data;
+    J.h = in.height;
+    J.w = in.width;
+    J.ho = out.height;
+    J.wo = out.width;
+    J.src_pitch = in.pitch / 4;
+    J.dst_pitch = out.pitch / 4;
+    J.cin = sg.cin;
+    J.cmid = sg.cmid;
+    J.cout = sg.cout;
+    J.flip = sg.flip;
+    J.pro = sg.pro;
+    J.epi = sg.epi;
+    const double sigma = sg.core_p[0];
+    const int r = (int)ceil(3.0 * sigma);
+    if (r < 1 || r > MP_MAX_RADIUS) return MP_ERROR_TOO_LARGE;
+    J.radius = r;
+    double e[MP_MAX_TAPS], sum = 0.0;
+    for (int k = -r; k <= r; ++k) {
+        e[k + r] = exp(-(double)(k * k) / (2.0 * sigma * sigma));
+        sum += e[k + r];
+    }
+    for (int k = 0; k < 2 * r + 1; ++k) J.wts[k] = (float)(e[k] / sum);
+    J.tw = sw;
+    J.th = rs;
+    J.tiles_x = (in.width + sw - 1) / sw;
+    J.ntiles = J.tiles_x * ((in.height + rs - 1) / rs);
+    J.vec_out = (out.pitch % 16) == 0 && ((uintptr_t)out.data % 16) == 0;
+    mp_encode_tiled_fn enc = mp_get_encode_tiled();
+    if (!enc) return MP_ERROR_UNSUPPORTED_TYPE;
+    cuuint64_t gdim[2] = {(cuuint64_t)in.width * (cuuint64_t)sg.cin, (cuuint64_t)in.height};
+    cuuint64_t gstr[1] = {(cuuint64_t)in.pitch};
+    cuuint32_t box[2] = {(cuuint32_t)mp_gs_boxw(sg.cin), (cuuint32_t)mp_gs_rb(sg.cmid)};
+    cuuint32_t es[2] = {1u, 1u};
+    CUresult cr = enc(&J.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)in.data, gdim, gstr, box, es,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return MP_ERROR_UNSUPPORTED_TYPE;
+    J.use_tma = 1;
+    return MILLIPYDE_SUCCESS;
+}
+
+// Streaming launch geometry for a launch whose largest radius is rmax;
+// false if the kernel cannot take it (the tile kernel runs instead).
+static bool mp_stream_setup(int cin, int cmid, int rmax, GsGeom *g, int *grid)
+{
+    *g = mp_gs_geom(mp_stream_stages(cmid), mp_gs_bucket(rmax), cin, cmid);
+    if ((size_t)g->total + 128 > (size_t)mp_max_smem_optin()) return false;
+    int cps = 0;
+    if (mp_gs_prepare(mp_variant(cin, cmid), (size_t)g->total + 128, &cps) != MILLIPYDE_SUCCESS) {
+        cudaGetLastError();
+        return false;
+    }
+    *grid = cps * mp_num_sms();
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Footprint-staged rotate (mp_rot.cu) selection.
+// ---------------------------------------------------------------------------
+// A ROTATE segment runs on the footprint-staged kernel when it has no
+// prologue and its source rows are TMA-legal.
+static bool mp_rot_ok(const Seg &sg, const MPImage &in)
+{
+    if (sg.kind != MPK_ROTATE || sg.pro.n != 0 || sg.cin != sg.cmid) return false;
+    if (sg.cin != 1 && sg.cin != 3 && sg.cin != 4) return false;
+    if ((in.pitch % 16) || ((uintptr_t)in.data % 16) || in.width <= 0 || in.height <= 0) return false;
+    return mp_get_encode_tiled() != nullptr;
+}
+
+static MPStatus mp_fill_job_rot(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out)
+{
+    MPStatus st = mp_fill_job(J, sg, in, out, 0, 0);   // source/destination, cos/sin, epilogue
+    if (st != MILLIPYDE_SUCCESS) return st;
+    const int C = sg.cin, TW = mp_ro_tw(C), TH = mp_ro_th(C);
+    J.tiles_x = (out.width + TW - 1) / TW;
+    J.ntiles = J.tiles_x * ((out.height + TH - 1) / TH);
+    // footprint of a tile: the rotated tile's bounding box plus the bilinear
+    // neighbour, in pixels; in floats plus up to 3 floats of alignment slack
+    const double c = fabs((double)J.cosq) / (double)(1LL << (MP_FIX_FRAC - 1));
+    const double sn = fabs((double)J.sinq) / (double)(1LL << (MP_FIX_FRAC - 1));
+    const int bw = (int)ceil((TW - 1) * c + (TH - 1) * sn + 1e-6) + 3;
+    const int bh = (int)ceil((TW - 1) * sn + (TH - 1) * c + 1e-6) + 3;
+    J.bxw = (bw * C + 3 + 3) & ~3;
+    J.byh = bh;
+    if (J.bxw > 256 || J.byh > 256) return MP_ERROR_TOO_LARGE;
+    mp_encode_tiled_fn enc = mp_get_encode_tiled();
+    if (!enc) return MP_ERROR_UNSUPPORTED_TYPE;
+    cuuint64_t gdim[2] = {(cuuint64_t)in.width * (cuuint64_t)C, (cuuint64_t)in.height};
+    cuuint64_t gstr[1] = {(cuuint64_t)in.pitch};
+    cuuint32_t box[2] = {(cuuint32_t)J.bxw, (cuuint32_t)J.byh};
+    cuuint32_t es[2] = {1u, 1u};
+    CUresult cr = enc(&J.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)in.data, gdim, gstr, box, es,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return MP_ERROR_UNSUPPORTED_TYPE;
+    J.use_tma = 1;
+    return MILLIPYDE_SUCCESS;
+}
+
+static int mp_rot_buf_floats(const MPJob &J) { return (J.bxw * J.byh + 31) & ~31; }
+
+// Persistent grid for a footprint-staged launch; false if it cannot run.
+static bool mp_rot_setup(int c, int buf_floats, int *grid)
+{
+    const size_t smem = mp_ro_smem(buf_floats);
+    if (smem > (size_t)mp_max_smem_optin()) return false;
+    int cps = 0;
+    if (mp_ro_prepare(c, smem, &cps) != MILLIPYDE_SUCCESS) {
+        cudaGetLastError();
+        return false;
+    }
+    *grid = cps * mp_num_sms();
+    return true;
+}
+
 static void mp_seg_tiles(const Seg &sg, int *tw, int *th)
 {
     *tw = *th = 0;
@@ -350,9 +527,45 @@ static size_t mp_seg_smem(const Seg &sg, int tw, int th)
 }
 
 // Runs one segment on one image with the job passed by value.
+static MPStatus mp_vh_run_single(const Seg &sg, const MPImage &in, const MPImage &out, cudaStream_t s,
+                                 bool *used);
+
 static MPStatus mp_run_segment_single(const Seg &sg, const MPImage &in, const MPImage &out,
                                       cudaStream_t s)
 {
+    {
+        bool used = false;
+        MPStatus st = mp_vh_run_single(sg, in, out, s, &used);
+        if (used || st != MILLIPYDE_SUCCESS) return st;
+    }
+    if (mp_rot_ok(sg, in)) {
+        MPJob J;
+        int grid = 0;
+        if (mp_fill_job_rot(J, sg, in, out) == MILLIPYDE_SUCCESS && mp_rot_setup(sg.cin, mp_rot_buf_floats(J), &grid)) {
+            int dev = 0;
+            cudaGetDevice(&dev);
+            int *err = mp_device_error_word(dev);
+            if (!err) return MP_ERROR_NO_DEVICE;
+            return mp_ro_launch_single(sg.cin, J, mp_rot_buf_floats(J), grid, err, s);
+        }
+    }
+    if (mp_stream_ok(sg, in)) {
+        GsGeom g;
+        int grid;
+        const int r = (int)ceil(3.0 * sg.core_p[0]);
+        if (r >= 1 && r <= MP_MAX_RADIUS && mp_stream_setup(sg.cin, sg.cmid, r, &g, &grid)) {
+            const long long strip_rows = (long long)((in.width + g.SW - 1) / g.SW) * in.height;
+            MPJob J;
+            MPStatus st = mp_fill_job_stream(J, sg, in, out, g.SW, mp_stream_rows(strip_rows, grid));
+            if (st == MILLIPYDE_SUCCESS) {
+                int dev = 0;
+                cudaGetDevice(&dev);
+                int *err = mp_device_error_word(dev);
+                if (!err) return MP_ERROR_NO_DEVICE;
+                return mp_gs_launch_single(mp_variant(sg.cin, sg.cmid), J, g, grid, err, s);
+            }
+        }
+    }
     int tw, th;
     mp_seg_tiles(sg, &tw, &th);
     MPJob J;
@@ -374,6 +587,8 @@ struct MPLaunch {
     size_t smem;
     double bytes;   // algorithmic bytes: inputs read once + outputs written once
     int gauss[4];   // GAUSS: tile width, tile height, largest radius, all sources TMA-able
+    GsGeom gs;      // GSTREAM: shared-memory geometry
+    int grid;       // GSTREAM: persistent CTAs
 };
 
 struct MPPlanImpl {
@@ -405,6 +620,7 @@ struct MPTables {
                  std::vector<MPJob> &js, double bytes)
     {
         MPLaunch L;
+        memset(&L, 0, sizeof(L));
         L.kind = kind;
         L.variant = variant;
         L.job_off = jobs.size();
@@ -431,7 +647,7 @@ struct MPTables {
             L.njobs++;
         }
         if (L.njobs == 0) return MILLIPYDE_SUCCESS;
-        if (kind < MPK_POINT_ADJ) {
+        if (kind < MPK_POINT_ADJ && kind != MPK_GSTREAM && kind != MPK_RSTREAM && kind != MPK_VH) {
             MPStatus e = mp_prepare_kind(kind, variant, smem);
             if (e != MILLIPYDE_SUCCESS) return e;
         }
@@ -454,6 +670,84 @@ struct MPTables {
         return mp_cuda_status(cudaMemcpyAsync(P->tables, host.data(), jb + tb, cudaMemcpyHostToDevice, s));
     }
 };
+
+// ---------------------------------------------------------------------------
+// Single-channel streaming gaussian (mp_vh.cuh) selection and jobs.
+// ---------------------------------------------------------------------------
+// A GAUSS segment runs on the single-channel kernel when the channel count
+// after its prologue is 1, its radius is compiled there, its epilogue keeps
+// one channel and its source rows are 8-byte aligned.
+static bool mp_vh_ok(const Seg &sg, const MPImage &in)
+{
+    if (sg.kind != MPK_GAUSS || sg.cmid != 1 || sg.cout != 1) return false;
+    if (sg.cin != 1 && sg.cin != 3 && sg.cin != 4) return false;
+    const int r = (int)ceil(3.0 * sg.core_p[0]);
+    if (r < 1 || r > MP_VH_RMAX) return false;
+    for (int i = 0; i < sg.epi.n; ++i)
+        if (sg.epi.op[i].op == MP_OP_RGB2GREY) return false;
+    return (in.pitch % 16) == 0 && ((uintptr_t)in.data % 16) == 0 && in.width > 0 && in.height > 0 &&
+           mp_get_encode_tiled() != nullptr;
+}
+
+static MPStatus mp_fill_job_vh(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out, int rs)
+{
+    MPStatus st = mp_fill_job(J, sg, in, out, 8, 8);   // radius, taps, pro/epilogue, flip
+    if (st != MILLIPYDE_SUCCESS) return st;
+    const int sw = mp_vh_fit_strip(J.radius, in.width);
+    J.tw = sw;
+    J.th = rs;
+    J.tiles_x = (in.width + sw - 1) / sw;
+    J.ntiles = J.tiles_x * ((in.height + rs - 1) / rs);
+    J.vec_out = (out.pitch % 16) == 0 && ((uintptr_t)out.data % 16) == 0;
+    // source map: boxes of 64 pixels x 8 rows (one per warp and staged group)
+    mp_encode_tiled_fn enc = mp_get_encode_tiled();
+    if (!enc) return MP_ERROR_UNSUPPORTED_TYPE;
+    cuuint64_t gdim[2] = {(cuuint64_t)in.width * (cuuint64_t)sg.cin, (cuuint64_t)in.height};
+    cuuint64_t gstr[1] = {(cuuint64_t)in.pitch};
+    cuuint32_t box[2] = {(cuuint32_t)(64 * sg.cin), 8u};
+    cuuint32_t es[2] = {1u, 1u};
+    CUresult cr = enc(&J.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)in.data, gdim, gstr, box, es,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return MP_ERROR_UNSUPPORTED_TYPE;
+    J.use_tma = 1;
+    return MILLIPYDE_SUCCESS;
+}
+
+// Rows per strip item: about four items per resident CTA over the launch,
+// at least 32 rows (the 2R head rows of an item are loads only).
+static int mp_vh_rows(long long strip_rows, int grid)
+{
+    const long long target = 4LL * (grid > 0 ? grid : 1);
+    long long rs = (strip_rows + target - 1) / target;
+    if (rs < 32) rs = 32;
+    if (rs > 4096) rs = 4096;
+    return (int)((rs + 7) / 8 * 8);
+}
+
+// One gaussian segment on one image with the single-channel kernel.
+static MPStatus mp_vh_run_single(const Seg &sg, const MPImage &in, const MPImage &out, cudaStream_t s, bool *used)
+{
+    *used = false;
+    if (!mp_vh_ok(sg, in)) return MILLIPYDE_SUCCESS;
+    int cps = 0;
+    if (mp_vh_prepare(sg.cin, &cps) != MILLIPYDE_SUCCESS) {
+        cudaGetLastError();
+        return MILLIPYDE_SUCCESS;
+    }
+    const int grid = cps * mp_num_sms();
+    const int r = (int)ceil(3.0 * sg.core_p[0]);
+    const int sw = mp_vh_fit_strip(r, in.width);
+    MPJob J;
+    MPStatus st = mp_fill_job_vh(J, sg, in, out, mp_vh_rows((long long)((in.width + sw - 1) / sw) * in.height, grid));
+    if (st != MILLIPYDE_SUCCESS) return st;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int *err = mp_device_error_word(dev);
+    if (!err) return MP_ERROR_NO_DEVICE;
+    *used = true;
+    return mp_vh_launch_single(sg.cin, J, grid, err, s);
+}
 
 static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage *in,
                               const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
@@ -560,7 +854,123 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             int kind = segs[ch.imgs[0]][k].kind;
             int tw = 0, th = 0;
             size_t smem = 0;
+            if (kind == MPK_ROTATE) {
+                // footprint-staged kernel when every image of the launch can take it
+                bool ok = true;
+                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
+                    const MPImage &src = (k == 0) ? in[ch.imgs[q]] : inter[q][k - 1];
+                    ok = mp_rot_ok(segs[ch.imgs[q]][k], src);
+                }
+                std::vector<MPJob> js;
+                double bytes = 0.0;
+                int bufmax = 0;
+                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
+                    const int img = ch.imgs[q];
+                    const Seg &sg = segs[img][k];
+                    const MPImage &src = (k == 0) ? in[img] : inter[q][k - 1];
+                    const MPImage &dst = (k + 1 == nseg) ? out[img] : inter[q][k];
+                    MPJob J;
+                    if (mp_fill_job_rot(J, sg, src, dst) != MILLIPYDE_SUCCESS) {
+                        ok = false;
+                        break;
+                    }
+                    bufmax = std::max(bufmax, mp_rot_buf_floats(J));
+                    bytes += 4.0 * ((double)src.height * src.width * src.channels +
+                                    (double)dst.height * dst.width * dst.channels);
+                    js.push_back(J);
+                }
+                int grid = 0;
+                const int c0 = segs[ch.imgs[0]][k].cin;
+                if (ok && mp_rot_setup(c0, bufmax, &grid)) {
+                    const size_t nl = P->launches.size();
+                    st = T.add(P->launches, MPK_RSTREAM, c0, mp_ro_smem(bufmax), js, bytes);
+                    if (st != MILLIPYDE_SUCCESS) return st;
+                    if (P->launches.size() > nl) {
+                        P->launches.back().grid = grid;
+                        P->launches.back().gauss[0] = bufmax;
+                    }
+                    continue;
+                }
+            }
             if (kind == MPK_GAUSS) {
+                // single-channel streaming kernel when every image of the launch can take it
+                bool ok = true;
+                long long strip_rows = 0;
+                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
+                    const Seg &sg = segs[ch.imgs[q]][k];
+                    const MPImage &src = (k == 0) ? in[ch.imgs[q]] : inter[q][k - 1];
+                    ok = mp_vh_ok(sg, src);
+                    const int sw = mp_vh_fit_strip((int)ceil(3.0 * sg.core_p[0]), src.width);
+                    strip_rows += (long long)((src.width + sw - 1) / sw) * src.height;
+                }
+                int cps = 0;
+                const int c0 = segs[ch.imgs[0]][k].cin;
+                if (ok && mp_vh_prepare(c0, &cps) == MILLIPYDE_SUCCESS) {
+                    const int grid = cps * mp_num_sms();
+                    const int rs = mp_vh_rows(strip_rows, grid);
+                    std::vector<MPJob> js;
+                    double bytes = 0.0;
+                    for (size_t q = 0; q < ch.imgs.size(); ++q) {
+                        const int img = ch.imgs[q];
+                        const MPImage &src = (k == 0) ? in[img] : inter[q][k - 1];
+                        const MPImage &dst = (k + 1 == nseg) ? out[img] : inter[q][k];
+                        MPJob J;
+                        st = mp_fill_job_vh(J, segs[img][k], src, dst, rs);
+                        if (st != MILLIPYDE_SUCCESS) return st;
+                        bytes += 4.0 * ((double)src.height * src.width * src.channels +
+                                        (double)dst.height * dst.width * dst.channels);
+                        js.push_back(J);
+                    }
+                    const size_t nl = P->launches.size();
+                    st = T.add(P->launches, MPK_VH, c0, 0, js, bytes);
+                    if (st != MILLIPYDE_SUCCESS) return st;
+                    if (P->launches.size() > nl) P->launches.back().grid = grid;
+                    continue;
+                }
+                cudaGetLastError();
+            }
+            if (kind == MPK_GAUSS) {
+                // streaming kernel when every image of the launch can take it
+                bool ok = true;
+                int srmax = 0;
+                long long strip_rows = 0;
+                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
+                    const Seg &sg = segs[ch.imgs[q]][k];
+                    const MPImage &src = (k == 0) ? in[ch.imgs[q]] : inter[q][k - 1];
+                    ok = mp_stream_ok(sg, src);
+                    srmax = std::max(srmax, (int)ceil(3.0 * sg.core_p[0]));
+                }
+                const Seg &s0 = segs[ch.imgs[0]][k];
+                GsGeom g;
+                int grid = 0;
+                if (ok && srmax <= MP_MAX_RADIUS && mp_stream_setup(s0.cin, s0.cmid, srmax, &g, &grid)) {
+                    for (int img : ch.imgs)
+                        strip_rows += (long long)((segs[img][k].win + g.SW - 1) / g.SW) * segs[img][k].hin;
+                    const int rs = mp_stream_rows(strip_rows, grid);
+                    std::vector<MPJob> js;
+                    double bytes = 0.0;
+                    for (size_t q = 0; q < ch.imgs.size(); ++q) {
+                        const int img = ch.imgs[q];
+                        const Seg &sg = segs[img][k];
+                        const MPImage &src = (k == 0) ? in[img] : inter[q][k - 1];
+                        const MPImage &dst = (k + 1 == nseg) ? out[img] : inter[q][k];
+                        MPJob J;
+                        st = mp_fill_job_stream(J, sg, src, dst, g.SW, rs);
+                        if (st != MILLIPYDE_SUCCESS) return st;
+                        bytes += 4.0 * ((double)src.height * src.width * src.channels +
+                                        (double)dst.height * dst.width * dst.channels);
+                        js.push_back(J);
+                    }
+                    const size_t nl = P->launches.size();
+                    st = T.add(P->launches, MPK_GSTREAM, mp_variant(s0.cin, s0.cmid), (size_t)g.total + 128, js,
+                               bytes);
+                    if (st != MILLIPYDE_SUCCESS) return st;
+                    if (P->launches.size() > nl) {
+                        P->launches.back().gs = g;
+                        P->launches.back().grid = grid;
+                    }
+                    continue;
+                }
                 int rmax = 0, cinm = 1, cmidm = 1, pro = 0;
                 for (int img : ch.imgs) {
                     const Seg &sg = segs[img][k];
@@ -593,15 +1003,28 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
     return T.upload(P, s);
 }
 
+static MPStatus mp_plan_launch_one(const MPPlanImpl *P, const MPLaunch &L, cudaStream_t s)
+{
+    if (L.kind >= MPK_POINT_ADJ)
+        return mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles,
+                                 P->err, s);
+    if (L.kind == MPK_VH)
+        return mp_vh_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles, L.grid,
+                            P->err, s);
+    if (L.kind == MPK_RSTREAM)
+        return mp_ro_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles,
+                            L.gauss[0], L.grid, P->err, s);
+    if (L.kind == MPK_GSTREAM)
+        return mp_gs_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles, L.gs,
+                            L.grid, P->err, s);
+    return mp_launch_kind(L.kind, L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles,
+                          L.smem, P->err, s, L.gauss);
+}
+
 static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
 {
     for (const MPLaunch &L : P->launches) {
-        MPStatus st = L.kind >= MPK_POINT_ADJ
-                          ? mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off,
-                                              L.total_tiles, P->err, s)
-                          : mp_launch_kind(L.kind, L.variant, P->jobs_dev + L.job_off,
-                                           P->tiles_dev + L.tile_off, L.total_tiles, L.smem, P->err, s,
-                                           L.gauss);
+        MPStatus st = mp_plan_launch_one(P, L, s);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -655,13 +1078,7 @@ MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream)
     const MPPlanImpl *P = (const MPPlanImpl *)plan;
     if (first < 0 || count < 0 || first + count > (int)P->launches.size()) return MP_ERROR_INVALID_ARGS;
     for (int i = first; i < first + count; ++i) {
-        const MPLaunch &L = P->launches[i];
-        MPStatus st = L.kind >= MPK_POINT_ADJ
-                          ? mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off,
-                                              L.total_tiles, P->err, (cudaStream_t)stream)
-                          : mp_launch_kind(L.kind, L.variant, P->jobs_dev + L.job_off,
-                                           P->tiles_dev + L.tile_off, L.total_tiles, L.smem, P->err,
-                                           (cudaStream_t)stream, L.gauss);
+        MPStatus st = mp_plan_launch_one(P, P->launches[i], (cudaStream_t)stream);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -1624,8 +2041,23 @@ extern "C" MPStatus mpk_tune_get_gauss_tile(int cin, int cmid, int has_pro, int 
     return MILLIPYDE_SUCCESS;
 }
 
+extern "C" MPStatus mpk_tune_set_stream(int cmid, int stages)
+{
+    if ((cmid != 1 && cmid != 3 && cmid != 4) || stages < 2 || stages > MP_GS_MAXNS)
+        return MP_ERROR_INVALID_ARGS;
+    std::lock_guard<std::mutex> lk(mp_tune_mutex);
+    for (MPStreamTune &t : mp_stream_tune)
+        if (t.cmid == cmid) {
+            t.ns = stages;
+            return MILLIPYDE_SUCCESS;
+        }
+    mp_stream_tune.push_back({cmid, stages});
+    return MILLIPYDE_SUCCESS;
+}
+
 extern "C" void mpk_tune_clear(void)
 {
     std::lock_guard<std::mutex> lk(mp_tune_mutex);
     mp_tune_table.clear();
+    mp_stream_tune.clear();
 }

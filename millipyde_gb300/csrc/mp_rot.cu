@@ -1,0 +1,255 @@
+// mp_rot.cu -- the footprint-staged bilinear rotate (sm_103a).
+//
+// Same operator and the same arithmetic as the ROTATE tile kernel: output
+// pixel p samples the source at s = R(theta) (p - c) + c, c = (W/2, H/2)
+// (the reference's geometry, src/millipyde_image.cpp:114-139), with s in
+// 64-bit fixed point (MP_FIX_FRAC fractional bits) and the bilinear
+// fractions taken from its top 24 fractional bits; neighbours outside the
+// source contribute 0.  The sample positions, and so the results, are
+// bit-identical to the tile kernel's, which keeps the rotate adjoint an
+// exact transpose.
+//
+// What changes is where the neighbours come from.  For each TW x TH output
+// tile the kernel works out the source footprint (the bounding box of the
+// rotated tile plus the bilinear neighbour) and TMA copies that box into
+// shared memory; boxes that leave the source arrive as zeros, which is the
+// zero fill, so the gather has no bounds checks at all.  CTAs are
+// persistent and double-buffered: the footprint of a CTA's next tile is in
+// flight while the current one is sampled.
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "mp_internal.cuh"
+
+namespace {
+
+// Footprint box origin (pixels) of output tile lt of job J.
+__device__ __forceinline__ void ro_origin(const MPJob &J, int lt, int TW, int TH, int *bx, int *by, int *x0,
+                                          int *y0)
+{
+    const int ty = lt / J.tiles_x, tx = lt - ty * J.tiles_x;
+    *x0 = tx * TW;
+    *y0 = ty * TH;
+    const long long W = J.w, H = J.h;
+    const long long xa = 2LL * *x0 - W, xb = 2LL * (*x0 + TW - 1) - W;
+    const long long ya = 2LL * *y0 - H, yb = 2LL * (*y0 + TH - 1) - H;
+    const long long cq = J.cosq, sq = J.sinq;
+    // min over the four corners of sx = cq*X2 - sq*Y2 and sy = sq*X2 + cq*Y2
+    const long long sx_min = min(cq * xa, cq * xb) + min(-sq * ya, -sq * yb) + (W << (MP_FIX_FRAC - 1));
+    const long long sy_min = min(sq * xa, sq * xb) + min(cq * ya, cq * yb) + (H << (MP_FIX_FRAC - 1));
+    *bx = (int)(sx_min >> MP_FIX_FRAC);
+    *by = (int)(sy_min >> MP_FIX_FRAC);
+}
+
+template <int C>
+__device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uint64_t *bar)
+{
+    int bx, by, x0, y0;
+    ro_origin(J, lt, mp_ro_tw(C), mp_ro_th(C), &bx, &by, &x0, &y0);
+    const int xf = bx * C;
+    mp_mbar_arrive_expect_tx(bar, (uint32_t)(J.bxw * J.byh * 4));
+    mp_tma_load_2d(buf, &J.tmap, bar, xf & ~3, by);
+}
+
+// One output tile: every thread samples TW*TH/NT pixels, one column, rows
+// NT/TW apart.
+template <int C>
+__device__ __forceinline__ void ro_tile(const MPJob &J, int lt, const float *buf)
+{
+    constexpr int TW = mp_ro_tw(C), TH = mp_ro_th(C), NT = MP_RO_NT;
+    constexpr int RSTEP = NT / TW, NPX = TW * TH / NT;
+    int bx, by, x0, y0;
+    ro_origin(J, lt, TW, TH, &bx, &by, &x0, &y0);
+    const int delta = bx * C - ((bx * C) & ~3);
+    const int bxw = J.bxw;
+    const int x = x0 + (threadIdx.x & (TW - 1));
+    const int yf = y0 + threadIdx.x / TW;
+    const int wo = J.wo, ho = J.ho;
+    if (x >= wo) return;
+    const long long W = J.w, H = J.h, cq = J.cosq, sq = J.sinq;
+    const long long X2 = 2LL * x - W, Y2 = 2LL * yf - H;
+    // sample position relative to the box origin, MP_FIX_FRAC fixed point
+    long long rx = cq * X2 - sq * Y2 + (W << (MP_FIX_FRAC - 1)) - ((long long)bx << MP_FIX_FRAC);
+    long long ry = sq * X2 + cq * Y2 + (H << (MP_FIX_FRAC - 1)) - ((long long)by << MP_FIX_FRAC);
+    const long long stx = -2LL * RSTEP * sq, sty = 2LL * RSTEP * cq;
+    const PwFast epi = mp_pw_fast(J.epi);
+    float *const dst = J.dst;
+    const int dp = J.dst_pitch;
+    const int xo = J.flip ? (wo - 1 - x) : x;
+#pragma unroll
+    for (int i = 0; i < NPX; ++i) {
+        const int y = yf + RSTEP * i;
+        if (y < ho) {
+            const int lx = (int)(rx >> (MP_FIX_FRAC - 24));   // 8.24 fixed point, non-negative
+            const int ly = (int)(ry >> (MP_FIX_FRAC - 24));
+            const float fx = (float)(lx & 0xFFFFFF) * 5.9604644775390625e-8f;
+            const float fy = (float)(ly & 0xFFFFFF) * 5.9604644775390625e-8f;
+            const float *p0 = buf + (ly >> 24) * bxw + (lx >> 24) * C + delta;
+            const float *p1 = p0 + bxw;
+            const float gx = 1.0f - fx, gy = 1.0f - fy;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < C; ++k)
+                v[k] = gy * (gx * p0[k] + fx * p0[C + k]) + fy * (gx * p1[k] + fx * p1[C + k]);
+            float *drow = dst + (size_t)y * dp;
+            if (epi.n == 0) {
+#pragma unroll
+                for (int k = 0; k < C; ++k) drow[(size_t)xo * C + k] = v[k];
+            } else {
+                const int co = mp_pw_apply_f(epi, J.epi, v, C);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    if (k < co) drow[(size_t)xo * co + k] = v[k];
+            }
+        }
+        rx += stx;
+        ry += sty;
+    }
+}
+
+__device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
+{
+    return smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
+}
+
+// Persistent loop over tiles t = first, first + step, ... of a tile -> job map
+// (or of one job when `jobs` is null).  Buffer k & 1 holds tile k's footprint.
+template <int C>
+__device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, const MPJob *one, int total,
+                                       int buf_floats, int *err)
+{
+    extern __shared__ unsigned char mp_ro_smem[];
+    unsigned char *base = ro_base(mp_ro_smem);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(base);
+    float *bufs = reinterpret_cast<float *>(base + 128);
+    if (threadIdx.x == 0) {
+        mp_mbar_init(bars, 1);
+        mp_mbar_init(bars + 1, 1);
+        mp_fence_barrier_init();
+    }
+    __syncthreads();
+    const int first = blockIdx.x, step = gridDim.x;
+    auto job_of = [&](int t) -> const MPJob & { return one ? *one : jobs[__ldg(tile_job + t)]; };
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 2; ++k) {
+            const int t = first + k * step;
+            if (t >= total) break;
+            const MPJob &J = job_of(t);
+            if (!one) mp_tensormap_acquire(&J.tmap);
+            ro_issue<C>(J, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k);
+        }
+    }
+    int k = 0;
+    for (int t = first; t < total; t += step, ++k) {
+        const MPJob &J = job_of(t);
+        const int lt = one ? t : t - J.tile0;
+        const float *buf = bufs + (k & 1) * buf_floats;
+        const bool ok = mp_mbar_wait_bounded(bars + (k & 1), (uint32_t)(k >> 1) & 1u);
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) atomicExch(err, MP_KERR_TIMEOUT);
+            // drain the other buffer's copy if one was issued
+            if (t + step < total) mp_mbar_wait_bounded(bars + ((k + 1) & 1), (uint32_t)((k + 1) >> 1) & 1u);
+            return;
+        }
+        ro_tile<C>(J, lt, buf);
+        __syncthreads();   // buffer k & 1 is free again
+        if (threadIdx.x == 0) {
+            const int tn = t + 2 * step;
+            if (tn < total) {
+                const MPJob &Jn = job_of(tn);
+                if (!one) mp_tensormap_acquire(&Jn.tmap);
+                ro_issue<C>(Jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1));
+            }
+        }
+    }
+}
+
+}  // namespace
+
+#define MP_RO_KERNELS(NAME, C)                                                                       \
+    __global__ void __launch_bounds__(MP_RO_NT) NAME##_batch(const MPJob *__restrict__ jobs,        \
+                                                             const int *__restrict__ tile_job,      \
+                                                             int total, int buf_floats, int *err)   \
+    {                                                                                               \
+        ro_run<C>(jobs, tile_job, nullptr, total, buf_floats, err);                                  \
+    }                                                                                               \
+    __global__ void __launch_bounds__(MP_RO_NT)                                                     \
+        NAME##_single(const __grid_constant__ MPJob job, int buf_floats, int *err)                  \
+    {                                                                                               \
+        ro_run<C>(nullptr, nullptr, &job, job.ntiles, buf_floats, err);                              \
+    }
+
+MP_RO_KERNELS(mp_ro_c1, 1)
+MP_RO_KERNELS(mp_ro_c3, 3)
+MP_RO_KERNELS(mp_ro_c4, 4)
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static const void *mp_ro_fn(int c, bool single)
+{
+    switch (c) {
+    case 1: return single ? (const void *)mp_ro_c1_single : (const void *)mp_ro_c1_batch;
+    case 3: return single ? (const void *)mp_ro_c3_single : (const void *)mp_ro_c3_batch;
+    case 4: return single ? (const void *)mp_ro_c4_single : (const void *)mp_ro_c4_batch;
+    default: return nullptr;
+    }
+}
+
+size_t mp_ro_smem(int buf_floats) { return 128 + 2 * (size_t)buf_floats * 4 + 128; }
+
+MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
+{
+    static std::mutex mtx;
+    static std::vector<std::pair<const void *, int>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return mp_cuda_status(e);
+    for (int single = 0; single < 2; ++single) {
+        const void *fn = mp_ro_fn(c, single != 0);
+        if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
+        std::lock_guard<std::mutex> lk(mtx);
+        bool have = false;
+        for (auto &d : done)
+            if (d.first == fn && d.second == dev) have = true;
+        if (have) continue;
+        int optin = 0;
+        e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return mp_cuda_status(e);
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        if (e != cudaSuccess) return mp_cuda_status(e);
+        done.push_back({fn, dev});
+    }
+    if (ctas_per_sm) {
+        int n = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mp_ro_fn(c, false), MP_RO_NT, smem);
+        if (e != cudaSuccess) return mp_cuda_status(e);
+        if (n < 1) return MP_ERROR_TOO_LARGE;
+        *ctas_per_sm = n;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
+MPStatus mp_ro_launch(int c, const MPJob *jobs_dev, const int *tile_job, int total, int buf_floats, int grid,
+                      int *err, cudaStream_t s)
+{
+    if (total <= 0) return MILLIPYDE_SUCCESS;
+    const void *fn = mp_ro_fn(c, false);
+    if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
+    if (grid > total) grid = total;
+    if (grid < 1) grid = 1;
+    void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&total, (void *)&buf_floats, (void *)&err};
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_RO_NT), args, mp_ro_smem(buf_floats), s));
+}
+
+MPStatus mp_ro_launch_single(int c, const MPJob &job, int buf_floats, int grid, int *err, cudaStream_t s)
+{
+    if (job.ntiles <= 0) return MILLIPYDE_SUCCESS;
+    const void *fn = mp_ro_fn(c, true);
+    if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
+    if (grid > job.ntiles) grid = job.ntiles;
+    if (grid < 1) grid = 1;
+    void *args[] = {(void *)&job, (void *)&buf_floats, (void *)&err};
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_RO_NT), args, mp_ro_smem(buf_floats), s));
+}

@@ -1,0 +1,314 @@
+// mp_vh.cuh -- the single-channel separable gaussian as one streaming kernel
+// (sm_103a): vertical pass in registers, horizontal pass through a small
+// shared-memory tile.
+//
+// Same operator as the other gaussian kernels (zero-padded separable
+// correlation with normalised exp(-k^2 / 2 sigma^2) taps, radius
+// ceil(3 sigma); the reference's weights and padding are
+// src/millipyde_image.cpp:745-756 and :170-172, :218-221), for segments whose
+// channel count after the prologue is 1: an rgb2grey prologue on 3- or
+// 4-channel sources, or a 1-channel source with a pointwise prologue.
+//
+// A work item is a STRIP of at most 2*NT - 2*R4 output columns (R4 = R
+// rounded up to 4; the width is fitted to each image) by RS output rows.  Each thread owns two adjacent columns
+// of the strip plus its halo and walks down them:
+//   load   one thread copies the source rows of the strip, 8 at a time, by
+//          TMA (one box of 64 pixels per warp) into a double-buffered
+//          staging area, the next 8 rows in flight while the current ones
+//          are filtered; boxes that leave the image arrive as zeros, and
+//          pixels outside the image read as 0 after the prologue.
+//   V      a register window of 8 + 2R rows of (prologued) column pairs; each
+//          step produces 8 vertical outputs per column with packed f32x2
+//          FMAs, then slides the window by 8 rows.
+//   H      the 8 vertical rows go to a double-buffered shared tile; after one
+//          barrier every thread computes 8 consecutive horizontal outputs of
+//          one row from registers and applies the epilogue and fliplr map.
+// The radius is a compile-time parameter (one instance per radius 1..12).
+#pragma once
+#include "mp_internal.cuh"
+
+#define MP_VH_NT 128
+#define MP_VH_VR 8
+#define MP_VH_VW (2 * MP_VH_NT + 4)   // shared tile row stride (floats)
+
+namespace mp_vh {
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+// d = a * b + c on float pairs (one f32x2 instruction).
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<unsigned long long *>(&a)), "l"(*reinterpret_cast<unsigned long long *>(&b)),
+          "l"(*reinterpret_cast<unsigned long long *>(&c)));
+    return *reinterpret_cast<float2 *>(&d);
+}
+
+// Prologue of the two staged pixels -> one value each; in0 / in1 say
+// whether each pixel lies inside the image (zero otherwise, after the
+// prologue: the zero padding of the blur).
+template <int CIN>
+__device__ __forceinline__ float2 prologue(const float *slot, bool in0, bool in1, bool grey_only, const PwFast &pro,
+                                           const PwList &L)
+{
+    float r[2 * CIN];
+    if (CIN == 4) {
+        const float4 a = ld4(slot), b = ld4(slot + 4);
+        r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+        r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < CIN; ++k) {
+            const float2 t = *reinterpret_cast<const float2 *>(slot + 2 * k);
+            r[2 * k] = t.x;
+            r[2 * k + 1] = t.y;
+        }
+    }
+    float2 o;
+    if (CIN >= 3 && grey_only) {
+        o.x = fminf(1.0f, 0.2125f * r[0] + 0.7154f * r[1] + 0.0721f * r[2]);
+        o.y = fminf(1.0f, 0.2125f * r[CIN] + 0.7154f * r[CIN + 1] + 0.0721f * r[CIN + 2]);
+    } else {
+        float a[4] = {0.f, 0.f, 0.f, 0.f}, b[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < CIN; ++k) {
+            a[k] = r[k];
+            b[k] = r[CIN + k];
+        }
+        mp_pw_apply_f(pro, L, a, CIN);
+        mp_pw_apply_f(pro, L, b, CIN);
+        o.x = a[0];
+        o.y = b[0];
+    }
+    o.x = in0 ? o.x : 0.f;
+    o.y = in1 ? o.y : 0.f;
+    return o;
+}
+
+// Shared memory of one CTA (floats): 2 mbarriers + taps (64 floats), two
+// horizontal tiles [2][VR][VW], two staging buffers [2][NW][VR][64*CIN].
+__host__ __device__ constexpr int mp_vh_smem_floats(int cin)
+{
+    return 64 + 64 + 2 * MP_VH_VR * MP_VH_VW + 2 * MP_VH_VR * 2 * MP_VH_NT * cin;
+}
+
+// One strip item with compiled radius R.  The strip is J.tw output columns
+// wide (a multiple of 8, at most 2*NT - 2*R4); window rows are counted from
+// source row y0 - R8 (R8 = R rounded up to 4) so that every step of VR rows
+// is exactly one staged group.
+template <int CIN, int R>
+__device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32_t &gcount, int *err)
+{
+    constexpr int NT = MP_VH_NT, VR = MP_VH_VR, VW = MP_VH_VW, NW = NT / 32;
+    constexpr int NTAP = 2 * R + 1, R4 = (R + 3) & ~3, E = R4 - R;
+    constexpr int R8 = R4;                                // window row padding (2*R8 is a multiple of 8)
+    constexpr int D = R8 - R;                             // tap offset inside the window
+    constexpr int NWIN = VR + 2 * R8;
+    constexpr int NPRE = 2 * R8 / VR;                     // groups holding the window head
+    constexpr int NLD = (E + 8 + 2 * R + 3) / 4;
+    constexpr int BOXW = 64 * CIN;                        // staged floats per warp and row
+    constexpr int GF = NW * VR * BOXW;                    // staged floats per group
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    float *taps = smem + 64;
+    float *tile = smem + 128;
+    float *stg = tile + 2 * VR * VW;                      // [2][NW][VR][BOXW]
+
+    const int sy = lt / J.tiles_x, sx = lt - sy * J.tiles_x;
+    const int H = J.h, W = J.w;
+    const int swo = J.tw, ng = swo >> 3;
+    const int x0 = sx * swo, y0 = sy * J.th;
+    const int y1 = min(H, y0 + J.th);
+    const int nsteps = (y1 - y0 + VR - 1) / VR;
+    const int xv = x0 - R4 + 2 * tid;                     // this thread's first column
+    const bool in0 = xv >= 0 && xv < W, in1 = xv + 1 >= 0 && xv + 1 < W;
+    const int ybase = y0 - R8;                            // source row of window row 0
+
+    __syncthreads();   // the previous item is done with the taps, tiles and staging
+    if (tid < 64) taps[tid] = tid < NTAP ? J.wts[tid] : 0.f;
+    const PwFast pro = mp_pw_fast(J.pro);
+    const bool grey_only = J.pro.n == 1 && pro.op == MP_OP_RGB2GREY;
+    const PwFast epi = mp_pw_fast(J.epi);
+    const int flip = J.flip, wo = J.wo, dp = J.dst_pitch;
+    float *const dst = J.dst;
+    const uint32_t g0 = gcount;                           // CTA-wide group counter at item start
+    const int ngroups = NPRE + nsteps;
+
+    // thread 0: TMA of window group g (rows [VR g, VR g + VR)) into buffer (g0+g) & 1
+    auto issue = [&](int g) {
+        const uint32_t G = g0 + (uint32_t)g;
+        uint64_t *bar = bars + (G & 1u);
+        float *b = stg + (G & 1u) * GF;
+        mp_mbar_arrive_expect_tx(bar, (uint32_t)(GF * 4));
+        for (int w = 0; w < NW; ++w)
+            mp_tma_load_2d(b + w * VR * BOXW, &J.tmap, bar, (x0 - R4 + 64 * w) * CIN, ybase + VR * g);
+    };
+    // all threads: wait for group g; false after a timeout (error word set)
+    auto wait = [&](int g) -> bool {
+        const uint32_t G = g0 + (uint32_t)g;
+        const bool ok = mp_mbar_wait_bounded(bars + (G & 1u), (G >> 1) & 1u);
+        if (__syncthreads_and(ok)) return true;
+        if (tid == 0) atomicExch(err, MP_KERR_TIMEOUT);
+        return false;
+    };
+    // prologue of row j of group g for this thread's two pixels
+    auto row_value = [&](int g, int j) -> float2 {
+        const uint32_t G = g0 + (uint32_t)g;
+        const float *slot = stg + (G & 1u) * GF + (warp * VR + j) * BOXW + lane * 2 * CIN;
+        const bool rin = (unsigned)(ybase + VR * g + j) < (unsigned)H;
+        return prologue<CIN>(slot, in0 && rin, in1 && rin, grey_only, pro, J.pro);
+    };
+
+    if (tid == 0) {
+        mp_tensormap_acquire(&J.tmap);
+        issue(0);
+    }
+    __syncthreads();
+    float2 w2[NTAP];
+#pragma unroll
+    for (int m = 0; m < NTAP; ++m) w2[m] = make_float2(taps[m], taps[m]);
+
+    float2 win[NWIN];
+    bool alive = true;
+    // window head: rows 0 .. 2*R8-1 (groups 0 .. NPRE-1)
+#pragma unroll
+    for (int g = 0; g < NPRE; ++g) {
+        if (tid == 0) issue(g + 1);            // its buffer was read in iteration g - 1
+        alive = alive && wait(g);
+#pragma unroll
+        for (int j = 0; j < VR; ++j) win[VR * g + j] = row_value(g, j);
+        __syncthreads();
+    }
+
+    for (int s = 0; s <= nsteps; ++s) {
+        if (s < nsteps && alive) {
+            // ---- V: group NPRE + s = window rows 2*R8 .. 2*R8 + VR - 1
+            const int gB = NPRE + s;
+            if (tid == 0 && gB + 1 < ngroups) issue(gB + 1);   // buffer of group gB - 1, read last step
+            alive = wait(gB);
+#pragma unroll
+            for (int j = 0; j < VR; ++j) win[2 * R8 + j] = row_value(gB, j);
+            float *tb = tile + (s & 1) * (VR * VW) + 2 * tid;
+#pragma unroll
+            for (int o = 0; o < VR; ++o) {
+                float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < NTAP; ++k) a = fma2(w2[k], win[o + D + k], a);
+                *reinterpret_cast<float2 *>(tb + o * VW) = a;
+            }
+#pragma unroll
+            for (int k = 0; k < 2 * R8; ++k) win[k] = win[k + VR];
+        }
+        if (s >= 1 && alive) {
+            // ---- H: output rows of step s-1 from its shared tile
+            const int sb = s - 1;
+            const float *tr = tile + (sb & 1) * (VR * VW);
+            for (int i = tid; i < VR * ng; i += NT) {
+                const int rr = i & (VR - 1), g = i >> 3;
+                const int y = y0 + VR * sb + rr;
+                const int xo0 = x0 + 8 * g;
+                if (y >= y1 || xo0 >= W) continue;
+                const float *gp = tr + rr * VW + 8 * g;
+                float x[4 * NLD];
+#pragma unroll
+                for (int q = 0; q < NLD; ++q) {
+                    const float4 v = ld4(gp + 4 * q);
+                    x[4 * q] = v.x;
+                    x[4 * q + 1] = v.y;
+                    x[4 * q + 2] = v.z;
+                    x[4 * q + 3] = v.w;
+                }
+                float o[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+                    for (int m = 0; m < NTAP; ++m) {
+                        if (m & 1) a1 = fmaf(w2[m].x, x[E + k + m], a1);
+                        else a0 = fmaf(w2[m].x, x[E + k + m], a0);
+                    }
+                    o[k] = mp_pw_chan_f(epi, J.epi, a0 + a1, 0, 1);
+                }
+                float *drow = dst + (size_t)y * dp;
+                if (!flip && J.vec_out && xo0 + 8 <= W) {
+                    *reinterpret_cast<float4 *>(drow + xo0) = make_float4(o[0], o[1], o[2], o[3]);
+                    *reinterpret_cast<float4 *>(drow + xo0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (xo0 + k < W) drow[flip ? wo - 1 - (xo0 + k) : xo0 + k] = o[k];
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // after a timeout: let the copies still in flight (the last groups
+    // issued, one per buffer) land before the buffers are reused
+    if (!alive) {
+        for (int g = ngroups - 2; g < ngroups; ++g) {
+            if (g < 0) continue;
+            const uint32_t G = g0 + (uint32_t)g;
+            mp_mbar_wait_bounded(bars + (G & 1u), (G >> 1) & 1u);
+        }
+    }
+    gcount = g0 + (uint32_t)ngroups;
+}
+
+template <int CIN>
+__device__ __forceinline__ void vh_dispatch(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
+{
+    switch (J.radius) {
+#define MP_VH_CASE(RR) \
+    case RR: vh_item<CIN, RR>(J, lt, smem, gc, err); break;
+        MP_VH_CASE(1) MP_VH_CASE(2) MP_VH_CASE(3) MP_VH_CASE(4) MP_VH_CASE(5) MP_VH_CASE(6)
+        MP_VH_CASE(7) MP_VH_CASE(8) MP_VH_CASE(9) MP_VH_CASE(10) MP_VH_CASE(11) MP_VH_CASE(12)
+#undef MP_VH_CASE
+    default: break;   // the planner never sends other radii here
+    }
+}
+
+__device__ __forceinline__ float *vh_base(float4 *raw)
+{
+    unsigned char *p = reinterpret_cast<unsigned char *>(raw);
+    return reinterpret_cast<float *>(p + ((128 - (int)(mp_smem_addr(p) & 127)) & 127));
+}
+
+__device__ __forceinline__ void vh_init(float *smem)
+{
+    if (threadIdx.x == 0) {
+        uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+        mp_mbar_init(bars, 1);
+        mp_mbar_init(bars + 1, 1);
+        mp_fence_barrier_init();
+    }
+    __syncthreads();
+}
+
+}  // namespace mp_vh
+
+// Persistent kernels: CTA b takes strip items b, b + grid, ...
+#define MP_VH_KERNELS(NAME, CIN)                                                                     \
+    __global__ void __launch_bounds__(MP_VH_NT, 3) NAME##_batch(                                    \
+        const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int total, int *err)      \
+    {                                                                                               \
+        extern __shared__ float4 mp_vh_dsmem4[];                                                    \
+        float *smem = mp_vh::vh_base(mp_vh_dsmem4);                                                 \
+        mp_vh::vh_init(smem);                                                                       \
+        uint32_t gc = 0;                                                                            \
+        for (int t = blockIdx.x; t < total; t += gridDim.x) {                                       \
+            const MPJob &J = jobs[__ldg(tile_job + t)];                                             \
+            mp_vh::vh_dispatch<CIN>(J, t - J.tile0, smem, gc, err);                                 \
+        }                                                                                           \
+    }                                                                                               \
+    __global__ void __launch_bounds__(MP_VH_NT, 3)                                                  \
+        NAME##_single(const __grid_constant__ MPJob job, int *err)                                  \
+    {                                                                                               \
+        extern __shared__ float4 mp_vh_dsmem4[];                                                    \
+        float *smem = mp_vh::vh_base(mp_vh_dsmem4);                                                 \
+        mp_vh::vh_init(smem);                                                                       \
+        uint32_t gc = 0;                                                                            \
+        for (int t = blockIdx.x; t < job.ntiles; t += gridDim.x)                                    \
+            mp_vh::vh_dispatch<CIN>(job, t, smem, gc, err);                                         \
+    }
