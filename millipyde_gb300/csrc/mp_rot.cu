@@ -53,9 +53,10 @@ __device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uin
 }
 
 // One output tile: every thread samples TW*TH/NT pixels, one column, rows
-// NT/TW apart.
-template <int C>
-__device__ __forceinline__ void ro_tile(const MPJob &J, int lt, const float *buf)
+// NT/TW apart.  EK = epilogue kind (0 none, 1 one channel-preserving op,
+// 2 general list), decided once per tile.
+template <int C, int EK>
+__device__ __forceinline__ void ro_tile_k(const MPJob &J, int lt, const float *buf)
 {
     constexpr int TW = mp_ro_tw(C), TH = mp_ro_th(C), NT = MP_RO_NT;
     constexpr int RSTEP = NT / TW, NPX = TW * TH / NT;
@@ -74,13 +75,15 @@ __device__ __forceinline__ void ro_tile(const MPJob &J, int lt, const float *buf
     long long ry = sq * X2 + cq * Y2 + (H << (MP_FIX_FRAC - 1)) - ((long long)by << MP_FIX_FRAC);
     const long long stx = -2LL * RSTEP * sq, sty = 2LL * RSTEP * cq;
     const PwFast epi = mp_pw_fast(J.epi);
-    float *const dst = J.dst;
     const int dp = J.dst_pitch;
     const int xo = J.flip ? (wo - 1 - x) : x;
+    const int co = EK == 2 ? 0 : C;
+    float *drow = J.dst + (size_t)yf * dp + (size_t)xo * C;
+    const size_t rstride = (size_t)RSTEP * dp;
+    const bool full = y0 + TH <= ho;
 #pragma unroll
     for (int i = 0; i < NPX; ++i) {
-        const int y = yf + RSTEP * i;
-        if (y < ho) {
+        if (full || yf + RSTEP * i < ho) {
             const int lx = (int)(rx >> (MP_FIX_FRAC - 24));   // 8.24 fixed point, non-negative
             const int ly = (int)(ry >> (MP_FIX_FRAC - 24));
             const float fx = (float)(lx & 0xFFFFFF) * 5.9604644775390625e-8f;
@@ -92,20 +95,36 @@ __device__ __forceinline__ void ro_tile(const MPJob &J, int lt, const float *buf
 #pragma unroll
             for (int k = 0; k < C; ++k)
                 v[k] = gy * (gx * p0[k] + fx * p0[C + k]) + fy * (gx * p1[k] + fx * p1[C + k]);
-            float *drow = dst + (size_t)y * dp;
-            if (epi.n == 0) {
+            if (EK == 0) {
 #pragma unroll
-                for (int k = 0; k < C; ++k) drow[(size_t)xo * C + k] = v[k];
+                for (int k = 0; k < C; ++k) drow[k] = v[k];
+            } else if (EK == 1) {
+#pragma unroll
+                for (int k = 0; k < C; ++k) drow[k] = mp_pw_chan(epi.op, epi.p0, epi.p1, epi.p2, v[k], k, C);
             } else {
-                const int co = mp_pw_apply_f(epi, J.epi, v, C);
+                // general list: the output may have fewer channels
+                const int c2 = mp_pw_apply_f(epi, J.epi, v, C);
+                float *d = J.dst + (size_t)(yf + RSTEP * i) * dp + (size_t)xo * c2;
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
-                    if (k < co) drow[(size_t)xo * co + k] = v[k];
+                    if (k < c2) d[k] = v[k];
             }
         }
         rx += stx;
         ry += sty;
+        drow += rstride;
     }
+    (void)co;
+}
+
+template <int C>
+__device__ __forceinline__ void ro_tile(const MPJob &J, int lt, const float *buf)
+{
+    const int n = J.epi.n;
+    const int op = J.epi.op[0].op;
+    if (n == 0) ro_tile_k<C, 0>(J, lt, buf);
+    else if (n == 1 && op != MP_OP_RGB2GREY) ro_tile_k<C, 1>(J, lt, buf);
+    else ro_tile_k<C, 2>(J, lt, buf);
 }
 
 __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)

@@ -132,6 +132,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     const bool grey_only = J.pro.n == 1 && pro.op == MP_OP_RGB2GREY;
     const PwFast epi = mp_pw_fast(J.epi);
     const int flip = J.flip, wo = J.wo, dp = J.dst_pitch;
+    const bool vec = !flip && J.vec_out;
     float *const dst = J.dst;
     const uint32_t g0 = gcount;                           // CTA-wide group counter at item start
     const int ngroups = NPRE + nsteps;
@@ -153,12 +154,25 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
         if (tid == 0) atomicExch(err, MP_KERR_TIMEOUT);
         return false;
     };
-    // prologue of row j of group g for this thread's two pixels
-    auto row_value = [&](int g, int j) -> float2 {
+    // prologue of the VR rows of group g for this thread's two pixels, into
+    // win[w0 .. w0 + VR): the prologue kind is decided once per group
+    auto group_values = [&](int g, float2 *wdst) {
         const uint32_t G = g0 + (uint32_t)g;
-        const float *slot = stg + (G & 1u) * GF + (warp * VR + j) * BOXW + lane * 2 * CIN;
-        const bool rin = (unsigned)(ybase + VR * g + j) < (unsigned)H;
-        return prologue<CIN>(slot, in0 && rin, in1 && rin, grey_only, pro, J.pro);
+        const float *slot = stg + (G & 1u) * GF + warp * VR * BOXW + lane * 2 * CIN;
+        const int yr = ybase + VR * g;
+        if (CIN >= 3 && grey_only) {
+#pragma unroll
+            for (int j = 0; j < VR; ++j) {
+                const bool rin = (unsigned)(yr + j) < (unsigned)H;
+                wdst[j] = prologue<CIN>(slot + j * BOXW, in0 && rin, in1 && rin, true, pro, J.pro);
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < VR; ++j) {
+                const bool rin = (unsigned)(yr + j) < (unsigned)H;
+                wdst[j] = prologue<CIN>(slot + j * BOXW, in0 && rin, in1 && rin, false, pro, J.pro);
+            }
+        }
     };
 
     if (tid == 0) {
@@ -177,8 +191,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     for (int g = 0; g < NPRE; ++g) {
         if (tid == 0) issue(g + 1);            // its buffer was read in iteration g - 1
         alive = alive && wait(g);
-#pragma unroll
-        for (int j = 0; j < VR; ++j) win[VR * g + j] = row_value(g, j);
+        group_values(g, win + VR * g);
         __syncthreads();
     }
 
@@ -188,8 +201,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
             const int gB = NPRE + s;
             if (tid == 0 && gB + 1 < ngroups) issue(gB + 1);   // buffer of group gB - 1, read last step
             alive = wait(gB);
-#pragma unroll
-            for (int j = 0; j < VR; ++j) win[2 * R8 + j] = row_value(gB, j);
+            group_values(gB, win + 2 * R8);
             float *tb = tile + (s & 1) * (VR * VW) + 2 * tid;
 #pragma unroll
             for (int o = 0; o < VR; ++o) {
@@ -229,10 +241,14 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                         if (m & 1) a1 = fmaf(w2[m].x, x[E + k + m], a1);
                         else a0 = fmaf(w2[m].x, x[E + k + m], a0);
                     }
-                    o[k] = mp_pw_chan_f(epi, J.epi, a0 + a1, 0, 1);
+                    o[k] = a0 + a1;
+                }
+                if (epi.n) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) o[k] = mp_pw_chan_f(epi, J.epi, o[k], 0, 1);
                 }
                 float *drow = dst + (size_t)y * dp;
-                if (!flip && J.vec_out && xo0 + 8 <= W) {
+                if (vec && xo0 + 8 <= W) {
                     *reinterpret_cast<float4 *>(drow + xo0) = make_float4(o[0], o[1], o[2], o[3]);
                     *reinterpret_cast<float4 *>(drow + xo0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
                 } else {
