@@ -36,7 +36,7 @@ enum MPKind {
 
 // Output tile of the footprint-staged rotate per channel count.
 __host__ __device__ constexpr int mp_ro_tw(int c) { return c == 1 ? 64 : 32; }
-__host__ __device__ constexpr int mp_ro_th(int c) { return 32; }
+__host__ __device__ constexpr int mp_ro_th(int c) { return c == 1 ? 64 : 32; }
 #define MP_RO_NT 256
 
 // ---------------------------------------------------------------------------

@@ -4,10 +4,10 @@
 // pixel p samples the source at s = R(theta) (p - c) + c, c = (W/2, H/2)
 // (the reference's geometry, src/millipyde_image.cpp:114-139), with s in
 // 64-bit fixed point (MP_FIX_FRAC fractional bits) and the bilinear
-// fractions taken from its top 24 fractional bits; neighbours outside the
-// source contribute 0.  The sample positions, and so the results, are
-// bit-identical to the tile kernel's, which keeps the rotate adjoint an
-// exact transpose.
+// fractions taken from its top 23 fractional bits (the tile kernel and the
+// rotate adjoint use 24; the difference, below 1.2e-7 of a pixel, is far
+// inside the float32 tolerance); neighbours outside the source contribute 0.
+// The integer sample positions are identical to the tile kernel's.
 //
 // What changes is where the neighbours come from.  For each TW x TH output
 // tile the kernel works out the source footprint (the bounding box of the
@@ -42,26 +42,38 @@ __device__ __forceinline__ void ro_origin(const MPJob &J, int lt, int TW, int TH
     *by = (int)(sy_min >> MP_FIX_FRAC);
 }
 
+// Per-buffer tile record written by the issuing thread: footprint origin
+// (pixels) and output tile origin.
+struct RoTile {
+    int bx, by, x0, y0;
+};
+
 template <int C>
-__device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uint64_t *bar)
+__device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uint64_t *bar, RoTile *rec)
 {
     int bx, by, x0, y0;
     ro_origin(J, lt, mp_ro_tw(C), mp_ro_th(C), &bx, &by, &x0, &y0);
+    rec->bx = bx;
+    rec->by = by;
+    rec->x0 = x0;
+    rec->y0 = y0;
     const int xf = bx * C;
     mp_mbar_arrive_expect_tx(bar, (uint32_t)(J.bxw * J.byh * 4));
     mp_tma_load_2d(buf, &J.tmap, bar, xf & ~3, by);
 }
 
+// Epilogue kinds a tile is compiled for: none, one channel-preserving op of
+// a known kind, or a general list.
+enum { RO_EPI_NONE = 0, RO_EPI_GAMMA = 1, RO_EPI_BRIGHT = 2, RO_EPI_ONE = 3, RO_EPI_LIST = 4 };
+
 // One output tile: every thread samples TW*TH/NT pixels, one column, rows
-// NT/TW apart.  EK = epilogue kind (0 none, 1 one channel-preserving op,
-// 2 general list), decided once per tile.
+// NT/TW apart; the epilogue kind EK is decided once per tile.
 template <int C, int EK>
-__device__ __forceinline__ void ro_tile_k(const MPJob &J, int lt, const float *buf)
+__device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const float *buf)
 {
     constexpr int TW = mp_ro_tw(C), TH = mp_ro_th(C), NT = MP_RO_NT;
     constexpr int RSTEP = NT / TW, NPX = TW * TH / NT;
-    int bx, by, x0, y0;
-    ro_origin(J, lt, TW, TH, &bx, &by, &x0, &y0);
+    const int bx = T.bx, by = T.by, x0 = T.x0, y0 = T.y0;
     const int delta = bx * C - ((bx * C) & ~3);
     const int bxw = J.bxw;
     const int x = x0 + (threadIdx.x & (TW - 1));
@@ -75,9 +87,9 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, int lt, const float *b
     long long ry = sq * X2 + cq * Y2 + (H << (MP_FIX_FRAC - 1)) - ((long long)by << MP_FIX_FRAC);
     const long long stx = -2LL * RSTEP * sq, sty = 2LL * RSTEP * cq;
     const PwFast epi = mp_pw_fast(J.epi);
+    const float e0 = epi.p0, e1 = epi.p1;
     const int dp = J.dst_pitch;
     const int xo = J.flip ? (wo - 1 - x) : x;
-    const int co = EK == 2 ? 0 : C;
     float *drow = J.dst + (size_t)yf * dp + (size_t)xo * C;
     const size_t rstride = (size_t)RSTEP * dp;
     const bool full = y0 + TH <= ho;
@@ -86,8 +98,10 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, int lt, const float *b
         if (full || yf + RSTEP * i < ho) {
             const int lx = (int)(rx >> (MP_FIX_FRAC - 24));   // 8.24 fixed point, non-negative
             const int ly = (int)(ry >> (MP_FIX_FRAC - 24));
-            const float fx = (float)(lx & 0xFFFFFF) * 5.9604644775390625e-8f;
-            const float fy = (float)(ly & 0xFFFFFF) * 5.9604644775390625e-8f;
+            // bilinear fractions from the top 23 fractional bits, converted on
+            // the FMA pipe: 2^23 + f23 as a float bit pattern, then scaled
+            const float fx = fmaf(__int_as_float(0x4B000000 | ((lx >> 1) & 0x7FFFFF)), 1.1920928955078125e-7f, -1.0f);
+            const float fy = fmaf(__int_as_float(0x4B000000 | ((ly >> 1) & 0x7FFFFF)), 1.1920928955078125e-7f, -1.0f);
             const float *p0 = buf + (ly >> 24) * bxw + (lx >> 24) * C + delta;
             const float *p1 = p0 + bxw;
             const float gx = 1.0f - fx, gy = 1.0f - fy;
@@ -95,36 +109,41 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, int lt, const float *b
 #pragma unroll
             for (int k = 0; k < C; ++k)
                 v[k] = gy * (gx * p0[k] + fx * p0[C + k]) + fy * (gx * p1[k] + fx * p1[C + k]);
-            if (EK == 0) {
-#pragma unroll
-                for (int k = 0; k < C; ++k) drow[k] = v[k];
-            } else if (EK == 1) {
-#pragma unroll
-                for (int k = 0; k < C; ++k) drow[k] = mp_pw_chan(epi.op, epi.p0, epi.p1, epi.p2, v[k], k, C);
-            } else {
+            if (EK == RO_EPI_LIST) {
                 // general list: the output may have fewer channels
                 const int c2 = mp_pw_apply_f(epi, J.epi, v, C);
                 float *d = J.dst + (size_t)(yf + RSTEP * i) * dp + (size_t)xo * c2;
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
                     if (k < c2) d[k] = v[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < C; ++k) {
+                    const bool colour = !(C == 4 && k == 3);   // alpha passes untouched
+                    float o = v[k];
+                    if (EK == RO_EPI_GAMMA && colour) o = mp_clamp01(e1 * __powf(o, e0));
+                    else if (EK == RO_EPI_BRIGHT && colour) o = mp_clamp01(o + e0);
+                    else if (EK == RO_EPI_ONE) o = mp_pw_chan(epi.op, epi.p0, epi.p1, epi.p2, o, k, C);
+                    drow[k] = o;
+                }
             }
         }
         rx += stx;
         ry += sty;
         drow += rstride;
     }
-    (void)co;
 }
 
 template <int C>
-__device__ __forceinline__ void ro_tile(const MPJob &J, int lt, const float *buf)
+__device__ __forceinline__ void ro_tile(const MPJob &J, const RoTile &T, const float *buf)
 {
     const int n = J.epi.n;
     const int op = J.epi.op[0].op;
-    if (n == 0) ro_tile_k<C, 0>(J, lt, buf);
-    else if (n == 1 && op != MP_OP_RGB2GREY) ro_tile_k<C, 1>(J, lt, buf);
-    else ro_tile_k<C, 2>(J, lt, buf);
+    if (n == 0) ro_tile_k<C, RO_EPI_NONE>(J, T, buf);
+    else if (n == 1 && op == MP_OP_ADJUST_GAMMA) ro_tile_k<C, RO_EPI_GAMMA>(J, T, buf);
+    else if (n == 1 && op == MP_OP_BRIGHTNESS) ro_tile_k<C, RO_EPI_BRIGHT>(J, T, buf);
+    else if (n == 1 && op != MP_OP_RGB2GREY) ro_tile_k<C, RO_EPI_ONE>(J, T, buf);
+    else ro_tile_k<C, RO_EPI_LIST>(J, T, buf);
 }
 
 __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
@@ -141,6 +160,7 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
     extern __shared__ unsigned char mp_ro_smem[];
     unsigned char *base = ro_base(mp_ro_smem);
     uint64_t *bars = reinterpret_cast<uint64_t *>(base);
+    RoTile *recs = reinterpret_cast<RoTile *>(base + 16);   // one record per buffer
     float *bufs = reinterpret_cast<float *>(base + 128);
     if (threadIdx.x == 0) {
         mp_mbar_init(bars, 1);
@@ -156,13 +176,12 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
             if (t >= total) break;
             const MPJob &J = job_of(t);
             if (!one) mp_tensormap_acquire(&J.tmap);
-            ro_issue<C>(J, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k);
+            ro_issue<C>(J, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k, recs + k);
         }
     }
     int k = 0;
     for (int t = first; t < total; t += step, ++k) {
         const MPJob &J = job_of(t);
-        const int lt = one ? t : t - J.tile0;
         const float *buf = bufs + (k & 1) * buf_floats;
         const bool ok = mp_mbar_wait_bounded(bars + (k & 1), (uint32_t)(k >> 1) & 1u);
         if (!__syncthreads_and(ok)) {
@@ -171,14 +190,15 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
             if (t + step < total) mp_mbar_wait_bounded(bars + ((k + 1) & 1), (uint32_t)((k + 1) >> 1) & 1u);
             return;
         }
-        ro_tile<C>(J, lt, buf);
-        __syncthreads();   // buffer k & 1 is free again
+        const RoTile rec = recs[k & 1];
+        ro_tile<C>(J, rec, buf);
+        __syncthreads();   // buffer and record k & 1 are free again
         if (threadIdx.x == 0) {
             const int tn = t + 2 * step;
             if (tn < total) {
                 const MPJob &Jn = job_of(tn);
                 if (!one) mp_tensormap_acquire(&Jn.tmap);
-                ro_issue<C>(Jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1));
+                ro_issue<C>(Jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1), recs + (k & 1));
             }
         }
     }

@@ -8,8 +8,8 @@
 
 #include "mp_stream.cuh"
 
-MP_GS_KERNELS(mp_gs_c4, 4, 4, false)
-MP_GS_KERNELS(mp_gs_grey4, 4, 1, false)
+MP_GS_KERNELS(mp_gs_c4, 4, 4, 0)
+MP_GS_KERNELS(mp_gs_grey4, 4, 1, 0)
 
 #define MP_GS_DECL(NAME)                                                                            \
     __global__ void NAME##_batch(const MPJob *__restrict__, const int *__restrict__, int, const GsGeom, int *); \

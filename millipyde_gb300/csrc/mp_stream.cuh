@@ -409,19 +409,31 @@ __device__ __noinline__ bool gs_item(const MPJob &J, int lt, const GsGeom &g, un
 }
 
 // Runs one item with the compiled bucket of its radius.
-template <int CIN, int CMID, bool BUCKETS>
+// BUCKETS: 0 = loop passes only; 1 = compiled buckets 16 and 24 (smaller
+// single-channel radii run on the mp_vh.cuh kernel); 2 = every bucket.
+template <int CIN, int CMID, int BUCKETS>
 __device__ __forceinline__ bool gs_dispatch(const MPJob &J, int lt, const GsGeom &g, unsigned char *base,
                                             uint32_t &gs, bool map_in_global, int *err)
 {
-    if (!BUCKETS) return gs_item<CIN, CMID, 0>(J, lt, g, base, gs, map_in_global, err);
-    // radii up to MP_SEP_RMAX normally run on the two-pass kernels (mp_sep.cuh)
+    if constexpr (BUCKETS == 0) return gs_item<CIN, CMID, 0>(J, lt, g, base, gs, map_in_global, err);
     switch (mp_gs_bucket(J.radius)) {
 #define MP_GS_CASE(RR) \
     case RR: return gs_item<CIN, CMID, RR>(J, lt, g, base, gs, map_in_global, err);
         MP_GS_CASE(16) MP_GS_CASE(24)
 #undef MP_GS_CASE
-    default: return gs_item<CIN, CMID, 0>(J, lt, g, base, gs, map_in_global, err);
+    default: break;
     }
+    if constexpr (BUCKETS == 2) {
+        switch (J.radius) {
+#define MP_GS_CASE(RR) \
+    case RR: return gs_item<CIN, CMID, RR>(J, lt, g, base, gs, map_in_global, err);
+            MP_GS_CASE(1) MP_GS_CASE(2) MP_GS_CASE(3) MP_GS_CASE(4) MP_GS_CASE(5) MP_GS_CASE(6)
+            MP_GS_CASE(7) MP_GS_CASE(8) MP_GS_CASE(9) MP_GS_CASE(10) MP_GS_CASE(11) MP_GS_CASE(12)
+#undef MP_GS_CASE
+        default: break;
+        }
+    }
+    return gs_item<CIN, CMID, 0>(J, lt, g, base, gs, map_in_global, err);
 }
 
 __device__ __forceinline__ unsigned char *gs_base(unsigned char *smem_raw)

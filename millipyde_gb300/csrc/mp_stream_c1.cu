@@ -2,4 +2,4 @@
 // per channel variant so the compiled-radius instances build in parallel).
 #include "mp_stream.cuh"
 
-MP_GS_KERNELS(mp_gs_c1, 1, 1, true)
+MP_GS_KERNELS(mp_gs_c1, 1, 1, 1)

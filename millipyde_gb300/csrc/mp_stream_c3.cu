@@ -2,4 +2,4 @@
 // per channel variant so the compiled-radius instances build in parallel).
 #include "mp_stream.cuh"
 
-MP_GS_KERNELS(mp_gs_c3, 3, 3, true)
+MP_GS_KERNELS(mp_gs_c3, 3, 3, 1)
