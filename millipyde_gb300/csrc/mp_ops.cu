@@ -475,8 +475,10 @@ static MPStatus mp_fill_job_rot(MPJob &J, const Seg &sg, const MPImage &in, cons
     // neighbour, in pixels; in floats plus up to 3 floats of alignment slack
     const double c = fabs((double)J.cosq) / (double)(1LL << (MP_FIX_FRAC - 1));
     const double sn = fabs((double)J.sinq) / (double)(1LL << (MP_FIX_FRAC - 1));
-    const int bw = (int)ceil((TW - 1) * c + (TH - 1) * sn + 1e-6) + 3;
-    const int bh = (int)ceil((TW - 1) * sn + (TH - 1) * c + 1e-6) + 3;
+    // (+3: floor spread, bilinear neighbour, rounding; +1: the margin pixel
+    // before the footprint)
+    const int bw = (int)ceil((TW - 1) * c + (TH - 1) * sn + 1e-6) + 4;
+    const int bh = (int)ceil((TW - 1) * sn + (TH - 1) * c + 1e-6) + 4;
     J.bxw = (bw * C + 3 + 3) & ~3;
     J.byh = bh;
     if (J.bxw > 256 || J.byh > 256) return MP_ERROR_TOO_LARGE;

@@ -7,7 +7,8 @@
 // fractions taken from its top 23 fractional bits (the tile kernel and the
 // rotate adjoint use 24; the difference, below 1.2e-7 of a pixel, is far
 // inside the float32 tolerance); neighbours outside the source contribute 0.
-// The integer sample positions are identical to the tile kernel's.
+// Each thread's first sample position is computed exactly as the tile
+// kernel does; the following ones are stepped in 32-bit fixed point.
 //
 // What changes is where the neighbours come from.  For each TW x TH output
 // tile the kernel works out the source footprint (the bounding box of the
@@ -38,8 +39,10 @@ __device__ __forceinline__ void ro_origin(const MPJob &J, int lt, int TW, int TH
     // min over the four corners of sx = cq*X2 - sq*Y2 and sy = sq*X2 + cq*Y2
     const long long sx_min = min(cq * xa, cq * xb) + min(-sq * ya, -sq * yb) + (W << (MP_FIX_FRAC - 1));
     const long long sy_min = min(sq * xa, sq * xb) + min(cq * ya, cq * yb) + (H << (MP_FIX_FRAC - 1));
-    *bx = (int)(sx_min >> MP_FIX_FRAC);
-    *by = (int)(sy_min >> MP_FIX_FRAC);
+    // one pixel of margin before the footprint: the stepped positions may
+    // drift below the exact ones by a few 2^-24 pixel
+    *bx = (int)(sx_min >> MP_FIX_FRAC) - 1;
+    *by = (int)(sy_min >> MP_FIX_FRAC) - 1;
 }
 
 // Per-buffer tile record written by the issuing thread: footprint origin
@@ -82,10 +85,15 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
     if (x >= wo) return;
     const long long W = J.w, H = J.h, cq = J.cosq, sq = J.sinq;
     const long long X2 = 2LL * x - W, Y2 = 2LL * yf - H;
-    // sample position relative to the box origin, MP_FIX_FRAC fixed point
-    long long rx = cq * X2 - sq * Y2 + (W << (MP_FIX_FRAC - 1)) - ((long long)bx << MP_FIX_FRAC);
-    long long ry = sq * X2 + cq * Y2 + (H << (MP_FIX_FRAC - 1)) - ((long long)by << MP_FIX_FRAC);
-    const long long stx = -2LL * RSTEP * sq, sty = 2LL * RSTEP * cq;
+    // sample position relative to the box origin: exact in MP_FIX_FRAC fixed
+    // point for the thread's first pixel, then stepped in 8.24 fixed point
+    // (the step rounded down; the drift over NPX steps stays below
+    // NPX * 2^-24 pixel)
+    const long long rx0 = cq * X2 - sq * Y2 + (W << (MP_FIX_FRAC - 1)) - ((long long)bx << MP_FIX_FRAC);
+    const long long ry0 = sq * X2 + cq * Y2 + (H << (MP_FIX_FRAC - 1)) - ((long long)by << MP_FIX_FRAC);
+    int lx = (int)(rx0 >> (MP_FIX_FRAC - 24)), ly = (int)(ry0 >> (MP_FIX_FRAC - 24));
+    const int stx = (int)((-2LL * RSTEP * sq) >> (MP_FIX_FRAC - 24));
+    const int sty = (int)((2LL * RSTEP * cq) >> (MP_FIX_FRAC - 24));
     const PwFast epi = mp_pw_fast(J.epi);
     const float e0 = epi.p0, e1 = epi.p1;
     const int dp = J.dst_pitch;
@@ -96,8 +104,6 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
 #pragma unroll
     for (int i = 0; i < NPX; ++i) {
         if (full || yf + RSTEP * i < ho) {
-            const int lx = (int)(rx >> (MP_FIX_FRAC - 24));   // 8.24 fixed point, non-negative
-            const int ly = (int)(ry >> (MP_FIX_FRAC - 24));
             // bilinear fractions from the top 23 fractional bits, converted on
             // the FMA pipe: 2^23 + f23 as a float bit pattern, then scaled
             const float fx = fmaf(__int_as_float(0x4B000000 | ((lx >> 1) & 0x7FFFFF)), 1.1920928955078125e-7f, -1.0f);
@@ -128,8 +134,8 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
                 }
             }
         }
-        rx += stx;
-        ry += sty;
+        lx += stx;
+        ly += sty;
         drow += rstride;
     }
 }
