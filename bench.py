@@ -51,7 +51,8 @@ CONFIG = {"workload": "uniform batch: 256 x 1024x1024x3 float32 RGB, rgb2grey ->
           "images": N_IMG, "height": H, "width": W, "channels": CH,
           "l2": "inputs (3.2 GB) larger than L2 (129 MB); no flush between steps"}
 ORACLE_OPS = [("rgb2grey",), ("gaussian", SIGMA), ("rotate", ANGLE), ("adjust_gamma", GAMMA)]
-CPU_SAMPLE = 16          # images of the workload the CPU legs process per step
+CPU_SAMPLE = 64          # images of the workload the cpu_baseline leg times (one bounded sample)
+REF_SAMPLE = 16          # images per step of the reference arm (--impl reference)
 
 
 # ----------------------------------------------------------------- CPU legs
@@ -81,12 +82,12 @@ def run_reference(args):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    workers = min(cores, CPU_SAMPLE)
+    workers = min(cores, REF_SAMPLE)
     for _ in range(args.warmup):
-        cpu_rate(CPU_SAMPLE, workers)
+        cpu_rate(REF_SAMPLE, workers)
     vals, secs = [], []
     for _ in range(args.steps):
-        v, dt = cpu_rate(CPU_SAMPLE, workers)
+        v, dt = cpu_rate(REF_SAMPLE, workers)
         vals.append(v)
         secs.append(dt)
     v = statistics.mean(vals)
@@ -97,7 +98,7 @@ def run_reference(args):
             "config": CONFIG,
             "cpu_baseline": {"value": round(v, 3), "unit": "Mpix/s", "cores": workers, "kind": "port",
                              "sample": "%d of the 256 images per step, one process per image "
-                                       "(spawn pool of %d), FP64 numpy oracle" % (CPU_SAMPLE, workers)},
+                                       "(spawn pool of %d), FP64 numpy oracle" % (REF_SAMPLE, workers)},
             "e2e": {"value": round(v, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -119,7 +120,7 @@ class Clocks:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                                          "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
 
@@ -489,7 +490,7 @@ def main():
     global N_IMG
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--images", type=int, default=N_IMG,
