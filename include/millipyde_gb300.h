@@ -342,6 +342,9 @@ MPStatus mpk_tune_get_gauss_tile(int cin, int cmid, int has_pro, int radius, int
 /* TMA stage count (2..6) of the streaming gaussian for a channel count
  * after the prologue (1, 3 or 4). */
 MPStatus mpk_tune_set_stream(int cmid, int stages);
+/* Intermediate bytes one chunk of a fused batch may hold (at least 1 MB;
+ * default 48 MB): a batch runs as one launch per segment per chunk. */
+MPStatus mpk_tune_set_chunk_bytes(size_t bytes);
 void mpk_tune_clear(void);
 
 /* Differentiable chains on dense batches (the autograd path): B images of

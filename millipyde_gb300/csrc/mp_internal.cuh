@@ -391,7 +391,7 @@ int mp_vh_strip(int radius);
 int mp_vh_fit_strip(int radius, int w);
 MPStatus mp_vh_prepare(int cin, int *ctas_per_sm);
 MPStatus mp_vh_launch(int cin, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
-                      cudaStream_t s);
+                      int *counter, cudaStream_t s);
 MPStatus mp_vh_launch_single(int cin, const MPJob &job, int grid, int *err, cudaStream_t s);
 
 // Streaming gaussian (mp_stream.cu).  mp_gs_prepare raises the

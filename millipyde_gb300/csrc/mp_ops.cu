@@ -24,10 +24,12 @@
 // Reference degree->radian constant (src/millipyde_image.cpp:702).
 #define MP_DEG2RAD 0.01745329252
 
-// Intermediate bytes a chunk of a fused batch may hold, so that the
-// intermediates written by one segment are still in L2 (129 MB on GB300)
-// when the next segment reads them.
-#define MP_L2_CHUNK_BYTES (48u << 20)
+// Intermediate bytes a chunk of a fused batch may hold (one launch per
+// segment per chunk; mpk_tune_set_chunk_bytes changes it).  Measured on
+// GB300 (256 x 1024^2 RGB, grey -> gaussian -> rotate -> gamma): 48 MB
+// chunks (intermediates small enough for L2) 2.33 ms per step, 512 MB
+// chunks 1.49 ms -- fewer, longer launches win over L2 residency.
+static size_t mp_chunk_bytes = (size_t)512 << 20;
 
 struct ROp {
     int op;
@@ -599,6 +601,7 @@ struct MPPlanImpl {
     MPJob *jobs_dev = nullptr;
     int *tiles_dev = nullptr;
     void *scratch = nullptr;
+    int *counters = nullptr;   // one work counter per launch (dynamically scheduled kinds)
     int *err = nullptr;        // device error word the kernels report into
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -819,7 +822,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 size_t b = 0;
                 for (size_t k = 0; k + 1 < sg.size(); ++k)
                     b += (size_t)sg[k].hout * mp_round16((long long)sg[k].wout * sg[k].cout * 4);
-                if (!ch.imgs.empty() && bytes + b > MP_L2_CHUNK_BYTES) break;
+                if (!ch.imgs.empty() && bytes + b > mp_chunk_bytes) break;
                 bytes += b;
                 ch.imgs.push_back(order[i]);
                 ++i;
@@ -1002,17 +1005,31 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             if (st != MILLIPYDE_SUCCESS) return st;
         }
     }
-    return T.upload(P, s);
+    st = T.upload(P, s);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    if (!P->launches.empty()) {
+        const size_t cb = P->launches.size() * sizeof(int);
+        st = mp_malloc_async((void **)&P->counters, cb, s);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        st = mp_cuda_status(cudaMemsetAsync(P->counters, 0, cb, s));
+    }
+    return st;
 }
 
-static MPStatus mp_plan_launch_one(const MPPlanImpl *P, const MPLaunch &L, cudaStream_t s)
+static MPStatus mp_plan_launch_one(const MPPlanImpl *P, size_t idx, cudaStream_t s)
 {
+    const MPLaunch &L = P->launches[idx];
     if (L.kind >= MPK_POINT_ADJ)
         return mp_launch_adjoint(L.kind, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles,
                                  P->err, s);
-    if (L.kind == MPK_VH)
+    if (L.kind == MPK_VH) {
+        // items beyond the first one per CTA are handed out by a counter,
+        // zeroed before every launch (a memset node under graph capture)
+        MPStatus st = mp_cuda_status(cudaMemsetAsync(P->counters + idx, 0, sizeof(int), s));
+        if (st != MILLIPYDE_SUCCESS) return st;
         return mp_vh_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles, L.grid,
-                            P->err, s);
+                            P->err, P->counters + idx, s);
+    }
     if (L.kind == MPK_RSTREAM)
         return mp_ro_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles,
                             L.gauss[0], L.grid, P->err, s);
@@ -1025,8 +1042,8 @@ static MPStatus mp_plan_launch_one(const MPPlanImpl *P, const MPLaunch &L, cudaS
 
 static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
 {
-    for (const MPLaunch &L : P->launches) {
-        MPStatus st = mp_plan_launch_one(P, L, s);
+    for (size_t i = 0; i < P->launches.size(); ++i) {
+        MPStatus st = mp_plan_launch_one(P, i, s);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -1036,6 +1053,8 @@ static void mp_plan_free(MPPlanImpl *P, cudaStream_t s)
 {
     mp_free_async(P->tables, s);
     mp_free_async(P->scratch, s);
+    mp_free_async(P->counters, s);
+    P->counters = nullptr;
     P->tables = nullptr;
     P->jobs_dev = nullptr;
     P->tiles_dev = nullptr;
@@ -1080,7 +1099,7 @@ MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream)
     const MPPlanImpl *P = (const MPPlanImpl *)plan;
     if (first < 0 || count < 0 || first + count > (int)P->launches.size()) return MP_ERROR_INVALID_ARGS;
     for (int i = first; i < first + count; ++i) {
-        MPStatus st = mp_plan_launch_one(P, P->launches[i], (cudaStream_t)stream);
+        MPStatus st = mp_plan_launch_one(P, (size_t)i, (cudaStream_t)stream);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
     return MILLIPYDE_SUCCESS;
@@ -2054,6 +2073,14 @@ extern "C" MPStatus mpk_tune_set_stream(int cmid, int stages)
             return MILLIPYDE_SUCCESS;
         }
     mp_stream_tune.push_back({cmid, stages});
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_tune_set_chunk_bytes(size_t bytes)
+{
+    if (bytes < ((size_t)1 << 20)) return MP_ERROR_INVALID_ARGS;
+    std::lock_guard<std::mutex> lk(mp_tune_mutex);
+    mp_chunk_bytes = bytes;
     return MILLIPYDE_SUCCESS;
 }
 

@@ -7,7 +7,7 @@
 #include "mp_vh.cuh"
 
 #define MP_VH_DECL(NAME)                                                                             \
-    __global__ void NAME##_batch(const MPJob *__restrict__, const int *__restrict__, int, int *);    \
+    __global__ void NAME##_batch(const MPJob *__restrict__, const int *__restrict__, int, int *, int *); \
     __global__ void NAME##_single(const MPJob, int *);
 MP_VH_DECL(mp_vh_c1)
 MP_VH_DECL(mp_vh_c3)
@@ -69,14 +69,14 @@ MPStatus mp_vh_prepare(int cin, int *ctas_per_sm)
 }
 
 MPStatus mp_vh_launch(int cin, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
-                      cudaStream_t s)
+                      int *counter, cudaStream_t s)
 {
     if (total <= 0) return MILLIPYDE_SUCCESS;
     const void *fn = mp_vh_fn(cin, false);
     if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
     if (grid > total) grid = total;
     if (grid < 1) grid = 1;
-    void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&total, (void *)&err};
+    void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&total, (void *)&err, (void *)&counter};
     return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_VH_NT), args, mp_vh_smem(cin), s));
 }
 

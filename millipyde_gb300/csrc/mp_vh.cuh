@@ -307,15 +307,22 @@ __device__ __forceinline__ void vh_init(float *smem)
 // Persistent kernels: CTA b takes strip items b, b + grid, ...
 #define MP_VH_KERNELS(NAME, CIN)                                                                     \
     __global__ void __launch_bounds__(MP_VH_NT, 3) NAME##_batch(                                    \
-        const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int total, int *err)      \
+        const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int total, int *err,      \
+        int *counter)                                                                               \
     {                                                                                               \
         extern __shared__ float4 mp_vh_dsmem4[];                                                    \
+        __shared__ int next_item;                                                                   \
         float *smem = mp_vh::vh_base(mp_vh_dsmem4);                                                 \
         mp_vh::vh_init(smem);                                                                       \
         uint32_t gc = 0;                                                                            \
-        for (int t = blockIdx.x; t < total; t += gridDim.x) {                                       \
+        /* first item by CTA index, the rest from the launch's counter */                          \
+        for (int t = blockIdx.x; t < total;) {                                                      \
             const MPJob &J = jobs[__ldg(tile_job + t)];                                             \
             mp_vh::vh_dispatch<CIN>(J, t - J.tile0, smem, gc, err);                                 \
+            __syncthreads(); /* every thread has read next_item */                                  \
+            if (threadIdx.x == 0) next_item = (int)gridDim.x + atomicAdd(counter, 1);              \
+            __syncthreads();                                                                        \
+            t = next_item;                                                                          \
         }                                                                                           \
     }                                                                                               \
     __global__ void __launch_bounds__(MP_VH_NT, 3)                                                  \
