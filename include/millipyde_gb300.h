@@ -360,6 +360,12 @@ MPStatus mpk_chain_forward(const int *ops, int nops, const double *params, const
 MPStatus mpk_chain_backward(const int *ops, int nops, const double *params, const float *x,
                             const float *dy, float *dx, double *dparams, int B, int H, int W, int C,
                             void *stream);
+/* The same with param_mask[k] != 0 for every op k whose parameters want a
+ * gradient (null: all of them); ops whose mask is 0 skip their parameter
+ * passes (a gaussian's two d sigma passes). */
+MPStatus mpk_chain_backward_masked(const int *ops, int nops, const double *params, const float *x,
+                                   const float *dy, float *dx, double *dparams, const int *param_mask,
+                                   int B, int H, int W, int C, void *stream);
 
 /* Allocation-free batch.  No counterpart in the reference.  For callers that
  * cannot allocate device memory (GPU memory owned by another allocator or

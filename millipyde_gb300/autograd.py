@@ -13,8 +13,8 @@ Forward runs the fused batch path (mpk_chain_forward).  Backward
 (mpk_chain_backward) saves nothing but x and the parameters: it recomputes
 the forward intermediates image chunk by image chunk (bounded scratch) and
 runs the adjoints in reverse -- one pass for each run of pointwise ops
-(with their parameter gradients), blur(g) and two derivative-tap dot passes
-for gaussian (d sigma), the exact transpose of the bilinear gather plus
+(with their parameter gradients), blur(g) and, when sigma requires grad, two
+derivative-tap dot passes for gaussian (d sigma), the exact transpose of the bilinear gather plus
 d theta for rotate, and the inverse permutation for transpose / fliplr.
 Parameter gradients accumulate in FP64.
 """
@@ -49,10 +49,10 @@ def _lib():
         L.mpk_chain_forward.restype = C.c_int
         L.mpk_chain_forward.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
-        L.mpk_chain_backward.restype = C.c_int
-        L.mpk_chain_backward.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
-                                         C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
-                                         C.c_void_p]
+        L.mpk_chain_backward_masked.restype = C.c_int
+        L.mpk_chain_backward_masked.argtypes = [C.POINTER(C.c_int), C.c_int, C.c_void_p, C.c_void_p,
+                                                C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int),
+                                                C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]
         _L = L
     return _L
 
@@ -96,8 +96,14 @@ class _ChainFn(torch.autograd.Function):
         dP = torch.zeros((B, max(1, nops), 3), dtype=torch.float64, device=x.device)
         L = _lib()
         stream = torch.cuda.current_stream(x.device).cuda_stream
-        _abi.check(L.mpk_chain_backward(_opcodes(ctx.names), nops, ctx.P.data_ptr(), x.data_ptr(),
-                                        gy.data_ptr(), dx.data_ptr(), dP.data_ptr(), B, H, W, Cc, stream))
+        # ops whose parameters want a gradient; the others skip their parameter passes
+        mask = (C.c_int * max(1, nops))()
+        for i, (k, _) in enumerate(ctx.slots):
+            if ctx.needs_input_grad[3 + i]:
+                mask[k] = 1
+        _abi.check(L.mpk_chain_backward_masked(_opcodes(ctx.names), nops, ctx.P.data_ptr(), x.data_ptr(),
+                                               gy.data_ptr(), dx.data_ptr(), dP.data_ptr(), mask,
+                                               B, H, W, Cc, stream))
         grads = []
         for (k, j), (shape, dtype, dev) in zip(ctx.slots, ctx.pshapes):
             g = dP[:, k, j]

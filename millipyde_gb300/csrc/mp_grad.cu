@@ -39,15 +39,6 @@ __device__ __forceinline__ float mp_block_sum(float v, float *red)
     return t;   // valid in thread 0
 }
 
-// One pointwise op forward (same arithmetic as mp_pw_apply).
-__device__ __forceinline__ int mp_pw_one(const PwOp &o, float v[4], int c)
-{
-    PwList L;
-    L.n = 1;
-    L.op[0] = o;
-    return mp_pw_apply(L, v, c);
-}
-
 // Back-propagates g (channels of the op's output) through op `o` whose input
 // was v (c channels).  Writes the input gradient to gi, adds parameter
 // gradients to pa[0..2].
@@ -115,50 +106,59 @@ __device__ __forceinline__ void mp_pw_back(const PwOp &o, const float v[4], int 
     }
 }
 
+// One 256 x 4 tile of a pointwise run.  The ops are walked by loops that
+// are not unrolled (one copy of each op's code): for op k from last to
+// first, its input is recomputed from x through ops 0..k-1 (runs are short),
+// then g is pulled back through op k.
 __device__ void mp_point_adj_tile(const MPJob &J, int t, float *red)
 {
     const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
     const int x = tx * 256 + threadIdx.x;
-    const int n = J.pro.n;
+    const int n = J.pro.n, cin = J.cin;
+    int cout = cin;
+    for (int k = 0; k < n; ++k)
+        if (J.pro.op[k].op == MP_OP_RGB2GREY && cout >= 3) cout = 1;
     float pacc[MP_MAX_PW][3];
 #pragma unroll
     for (int k = 0; k < MP_MAX_PW; ++k) pacc[k][0] = pacc[k][1] = pacc[k][2] = 0.f;
     if (x < J.w) {
+#pragma unroll 1
         for (int i = 0; i < 4; ++i) {
             const int y = ty * 4 + i;
             if (y >= J.h) break;
-            float v[MP_MAX_PW + 1][4];
-            int cs[MP_MAX_PW + 1];
-            const float *p = J.src + (size_t)y * J.src_pitch + (size_t)x * J.cin;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) v[0][c] = (c < J.cin) ? __ldg(p + c) : 0.f;
-            cs[0] = J.cin;
-#pragma unroll
-            for (int k = 0; k < MP_MAX_PW; ++k) {
-                if (k < n) {
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) v[k + 1][c] = v[k][c];
-                    cs[k + 1] = mp_pw_one(J.pro.op[k], v[k + 1], cs[k]);
-                }
-            }
-            float g[4];
-            const int cout = cs[n];
+            float x0[4], g[4];
+            const float *p = J.src + (size_t)y * J.src_pitch + (size_t)x * cin;
             const float *gp = J.aux + (size_t)y * J.aux_pitch + (size_t)x * cout;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) g[c] = (c < cout) ? __ldg(gp + c) : 0.f;
-#pragma unroll
-            for (int k = MP_MAX_PW - 1; k >= 0; --k) {
-                if (k < n) {
-                    float gi[4];
-                    mp_pw_back(J.pro.op[k], v[k], cs[k], g, gi, pacc[k]);
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) g[c] = gi[c];
-                }
+            for (int c = 0; c < 4; ++c) {
+                x0[c] = (c < cin) ? __ldg(p + c) : 0.f;
+                g[c] = (c < cout) ? __ldg(gp + c) : 0.f;
             }
-            float *d = J.dst + (size_t)y * J.dst_pitch + (size_t)x * J.cin;
+#pragma unroll 1
+            for (int k = n - 1; k >= 0; --k) {
+                float v[4] = {x0[0], x0[1], x0[2], x0[3]};
+                int c = cin;
+#pragma unroll 1
+                for (int j = 0; j < k; ++j) {
+                    const PwOp o = J.pro.op[j];
+                    c = mp_pw_op(o.op, o.p0, o.p1, o.p2, v, c);
+                }
+                float gi[4], pa[3] = {0.f, 0.f, 0.f};
+                mp_pw_back(J.pro.op[k], v, c, g, gi, pa);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) g[q] = gi[q];
+#pragma unroll
+                for (int kk = 0; kk < MP_MAX_PW; ++kk)
+                    if (kk == k) {
+                        pacc[kk][0] += pa[0];
+                        pacc[kk][1] += pa[1];
+                        pacc[kk][2] += pa[2];
+                    }
+            }
+            float *d = J.dst + (size_t)y * J.dst_pitch + (size_t)x * cin;
 #pragma unroll
             for (int c = 0; c < 4; ++c)
-                if (c < J.cin) d[c] = g[c];
+                if (c < cin) d[c] = g[c];
         }
     }
     if (!J.acc) return;
@@ -210,24 +210,36 @@ __device__ void mp_rotate_adj_tile(const MPJob &J, int t, float *red)
         const float pyf = -J.sth * dxq + J.cth * dyq + hh;
         const int px0 = (int)floorf(pxf) - 1, py0 = (int)floorf(pyf) - 1;
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int py = py0; py < py0 + 4; ++py) {
-            if (py < 0 || py >= J.h) continue;
-            for (int px = px0; px < px0 + 4; ++px) {
-                if (px < 0 || px >= J.w) continue;
-                long long sx, sy;
-                mp_rot_src(J, px, py, sx, sy);
+        // sample positions of the 4 x 4 candidates: the map is affine, so
+        // they step exactly by 2 cos / 2 sin from the first one
+        long long sxr, syr;
+        mp_rot_src(J, px0, py0, sxr, syr);
+        const long long c2 = 2 * J.cosq, s2 = 2 * J.sinq;
+#pragma unroll
+        for (int jy = 0; jy < 4; ++jy) {
+            const int py = py0 + jy;
+            const bool yok = py >= 0 && py < J.h;
+            long long sx = sxr, sy = syr;
+#pragma unroll
+            for (int jx = 0; jx < 4; ++jx) {
+                const int px = px0 + jx;
                 const int ix = (int)(sx >> MP_FIX_FRAC), iy = (int)(sy >> MP_FIX_FRAC);
                 const int ex = qx - ix, ey = qy - iy;
-                if ((unsigned)ex > 1u || (unsigned)ey > 1u) continue;
-                const float fx = mp_frac24(sx), fy = mp_frac24(sy);
-                const float wx = ex ? fx : 1.0f - fx;
-                const float wy = ey ? fy : 1.0f - fy;
-                const float w = wy * wx;
-                const float *gp = J.aux + (size_t)py * J.aux_pitch + (size_t)px * C;
+                if (yok && px >= 0 && px < J.w && (unsigned)ex <= 1u && (unsigned)ey <= 1u) {
+                    const float fx = mp_frac24(sx), fy = mp_frac24(sy);
+                    const float wx = ex ? fx : 1.0f - fx;
+                    const float wy = ey ? fy : 1.0f - fy;
+                    const float w = wy * wx;
+                    const float *gp = J.aux + (size_t)py * J.aux_pitch + (size_t)px * C;
 #pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    if (c < C) acc[c] = fmaf(w, __ldg(gp + c), acc[c]);
+                    for (int c = 0; c < 4; ++c)
+                        if (c < C) acc[c] = fmaf(w, __ldg(gp + c), acc[c]);
+                }
+                sx += c2;
+                sy += s2;
             }
+            sxr -= s2;
+            syr += c2;
         }
         float *d = J.dst + (size_t)qy * J.dst_pitch + (size_t)qx * C;
 #pragma unroll

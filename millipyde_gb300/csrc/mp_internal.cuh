@@ -25,8 +25,8 @@
 // whose epilogue is per-channel.
 // RSTREAM is the footprint-staged rotate (mp_rot.cu), used for ROTATE
 // segments without a prologue whose source rows are TMA-legal.
-// VH is the single-channel streaming gaussian (mp_vh.cuh), for radii up to
-// MP_VH_RMAX.
+// VH is the streaming gaussian of mp_vh.cuh (single-channel and
+// channel-preserving families), for radii up to MP_VH_RMAX.
 enum MPKind {
     MPK_POINT = 0, MPK_GAUSS = 1, MPK_ROTATE = 2, MPK_TRANSPOSE = 3, MPK_GSTREAM = 4, MPK_RSTREAM = 5,
     MPK_VH = 8
@@ -245,6 +245,65 @@ __device__ __forceinline__ float mp_pw_chan_f(const PwFast &f, const PwList &L, 
     return v;
 }
 
+// Up to three channel-preserving pointwise ops held in registers, applied to
+// N values at once (value k belongs to channel ch[k] of a cm-channel pixel):
+// the op kind is switched on once per op and group instead of once per
+// value.  Same arithmetic as mp_pw_chan; lists longer than three ops are
+// read from L.
+struct PwRegs {
+    int n;
+    int op[3];
+    float p0[3], p1[3], p2[3];
+};
+
+__device__ __forceinline__ PwRegs mp_pw_regs(const PwList &L)
+{
+    PwRegs r;
+    r.n = L.n;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        r.op[i] = L.op[i].op;
+        r.p0[i] = L.op[i].p0;
+        r.p1[i] = L.op[i].p1;
+        r.p2[i] = L.op[i].p2;
+    }
+    return r;
+}
+
+template <int N>
+__device__ __forceinline__ void mp_pw_chan_n(const PwRegs &f, const PwList &L, float (&v)[N], const int (&ch)[N],
+                                             int cm)
+{
+    if (f.n > 3) {
+        for (int i = 0; i < L.n; ++i)
+#pragma unroll
+            for (int k = 0; k < N; ++k) v[k] = mp_pw_chan(L.op[i].op, L.op[i].p0, L.op[i].p1, L.op[i].p2, v[k], ch[k], cm);
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (i >= f.n) break;
+        const float p0 = f.p0[i], p1 = f.p1[i], p2 = f.p2[i];
+        switch (f.op[i]) {
+        case MP_OP_BRIGHTNESS:
+#pragma unroll
+            for (int k = 0; k < N; ++k) v[k] = (cm == 4 && ch[k] == 3) ? v[k] : mp_clamp01(v[k] + p0);
+            break;
+        case MP_OP_ADJUST_GAMMA:
+#pragma unroll
+            for (int k = 0; k < N; ++k) v[k] = (cm == 4 && ch[k] == 3) ? v[k] : mp_clamp01(p1 * __powf(v[k], p0));
+            break;
+        case MP_OP_COLORIZE:
+#pragma unroll
+            for (int k = 0; k < N; ++k)
+                if (cm >= 3 && ch[k] < 3) v[k] = fminf(1.0f, v[k] * (ch[k] == 0 ? p0 : (ch[k] == 1 ? p1 : p2)));
+            break;
+        default:
+            break;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // mbarrier / TMA wrappers (PTX ISA 8.x, sm_90+; compiled for sm_103a).
 // ---------------------------------------------------------------------------
@@ -385,14 +444,19 @@ MPStatus mp_ro_launch(int c, const MPJob *jobs_dev, const int *tile_job, int tot
                       int *err, cudaStream_t s);
 MPStatus mp_ro_launch_single(int c, const MPJob &job, int buf_floats, int grid, int *err, cudaStream_t s);
 size_t mp_ro_smem(int buf_floats);
-// Single-channel streaming gaussian (mp_vh*.cu): strip width in output
-// pixels for a radius, resident CTAs per SM, launches.
-int mp_vh_strip(int radius);
-int mp_vh_fit_strip(int radius, int w);
-MPStatus mp_vh_prepare(int cin, int *ctas_per_sm);
-MPStatus mp_vh_launch(int cin, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
+// Streaming gaussian of mp_vh.cuh (mp_vh*.cu, mp_vc*.cu).  A kernel code
+// names the family: the source channel count (1, 3, 4) for the
+// single-channel family (cmid 1), 4 + C (7, 8) for the channel-preserving
+// family on C = 3 or 4 interleaved channels; -1 if neither takes
+// (cin, cmid).  Strips are counted in columns: pixels when cm = 1, floats of
+// the interleaved row otherwise.
+int mp_vh_code(int cin, int cmid);
+int mp_vh_strip(int radius, int cm);
+int mp_vh_fit_strip(int radius, int w, int cm);
+MPStatus mp_vh_prepare(int code, int *ctas_per_sm);
+MPStatus mp_vh_launch(int code, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
                       int *counter, cudaStream_t s);
-MPStatus mp_vh_launch_single(int cin, const MPJob &job, int grid, int *err, cudaStream_t s);
+MPStatus mp_vh_launch_single(int code, const MPJob &job, int grid, int *err, cudaStream_t s);
 
 // Streaming gaussian (mp_stream.cu).  mp_gs_prepare raises the
 // shared-memory limit and returns the resident CTAs per SM (call outside

@@ -679,13 +679,13 @@ struct MPTables {
 // ---------------------------------------------------------------------------
 // Single-channel streaming gaussian (mp_vh.cuh) selection and jobs.
 // ---------------------------------------------------------------------------
-// A GAUSS segment runs on the single-channel kernel when the channel count
-// after its prologue is 1, its radius is compiled there, its epilogue keeps
-// one channel and its source rows are 8-byte aligned.
+// A GAUSS segment runs on the mp_vh.cuh kernels when one of its families
+// takes its channels (1 after the prologue, or C = 3 / 4 kept throughout),
+// its radius is compiled there, its epilogue keeps the channel count and
+// its source rows are TMA-legal.
 static bool mp_vh_ok(const Seg &sg, const MPImage &in)
 {
-    if (sg.kind != MPK_GAUSS || sg.cmid != 1 || sg.cout != 1) return false;
-    if (sg.cin != 1 && sg.cin != 3 && sg.cin != 4) return false;
+    if (sg.kind != MPK_GAUSS || mp_vh_code(sg.cin, sg.cmid) < 0 || sg.cout != sg.cmid) return false;
     const int r = (int)ceil(3.0 * sg.core_p[0]);
     if (r < 1 || r > MP_VH_RMAX) return false;
     for (int i = 0; i < sg.epi.n; ++i)
@@ -698,18 +698,19 @@ static MPStatus mp_fill_job_vh(MPJob &J, const Seg &sg, const MPImage &in, const
 {
     MPStatus st = mp_fill_job(J, sg, in, out, 8, 8);   // radius, taps, pro/epilogue, flip
     if (st != MILLIPYDE_SUCCESS) return st;
-    const int sw = mp_vh_fit_strip(J.radius, in.width);
+    const int cm = mp_vh_code(sg.cin, sg.cmid) > 4 ? sg.cmid : 1;   // channels per pixel column
+    const int sw = mp_vh_fit_strip(J.radius, in.width, cm);           // in columns
     J.tw = sw;
     J.th = rs;
-    J.tiles_x = (in.width + sw - 1) / sw;
+    J.tiles_x = (in.width * cm + sw - 1) / sw;
     J.ntiles = J.tiles_x * ((in.height + rs - 1) / rs);
     J.vec_out = (out.pitch % 16) == 0 && ((uintptr_t)out.data % 16) == 0;
-    // source map: boxes of 64 pixels x 8 rows (one per warp and staged group)
+    // source map: boxes of 64 columns x 8 rows (one per warp and staged group)
     mp_encode_tiled_fn enc = mp_get_encode_tiled();
     if (!enc) return MP_ERROR_UNSUPPORTED_TYPE;
     cuuint64_t gdim[2] = {(cuuint64_t)in.width * (cuuint64_t)sg.cin, (cuuint64_t)in.height};
     cuuint64_t gstr[1] = {(cuuint64_t)in.pitch};
-    cuuint32_t box[2] = {(cuuint32_t)(64 * sg.cin), 8u};
+    cuuint32_t box[2] = {(cuuint32_t)(64 * (cm == 1 ? sg.cin : 1)), 8u};
     cuuint32_t es[2] = {1u, 1u};
     CUresult cr = enc(&J.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)in.data, gdim, gstr, box, es,
                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -735,23 +736,135 @@ static MPStatus mp_vh_run_single(const Seg &sg, const MPImage &in, const MPImage
 {
     *used = false;
     if (!mp_vh_ok(sg, in)) return MILLIPYDE_SUCCESS;
+    const int code = mp_vh_code(sg.cin, sg.cmid), cm = code > 4 ? sg.cmid : 1;
     int cps = 0;
-    if (mp_vh_prepare(sg.cin, &cps) != MILLIPYDE_SUCCESS) {
+    if (mp_vh_prepare(code, &cps) != MILLIPYDE_SUCCESS) {
         cudaGetLastError();
         return MILLIPYDE_SUCCESS;
     }
     const int grid = cps * mp_num_sms();
     const int r = (int)ceil(3.0 * sg.core_p[0]);
-    const int sw = mp_vh_fit_strip(r, in.width);
+    const int sw = mp_vh_fit_strip(r, in.width, cm);
     MPJob J;
-    MPStatus st = mp_fill_job_vh(J, sg, in, out, mp_vh_rows((long long)((in.width + sw - 1) / sw) * in.height, grid));
+    MPStatus st = mp_fill_job_vh(J, sg, in, out,
+                                 mp_vh_rows((long long)((in.width * cm + sw - 1) / sw) * in.height, grid));
     if (st != MILLIPYDE_SUCCESS) return st;
     int dev = 0;
     cudaGetDevice(&dev);
     int *err = mp_device_error_word(dev);
     if (!err) return MP_ERROR_NO_DEVICE;
     *used = true;
-    return mp_vh_launch_single(sg.cin, J, grid, err, s);
+    return mp_vh_launch_single(code, J, grid, err, s);
+}
+
+// Adds one launch of a gaussian stage over images (sgs[i]: srcs[i] ->
+// dsts[i]) with the fastest kernel that takes every image: the mp_vh.cuh
+// streaming kernels, the strip-streaming kernel, else the tile kernel.  The
+// images go into the job table in order of radius: work items are handed out
+// in table order, so the CTAs of an SM run one compiled radius at a time
+// instead of thrashing the instruction cache with all of them.
+static MPStatus mp_add_gauss_ordered(MPTables &T, std::vector<MPLaunch> &launches, const std::vector<Seg> &sgs,
+                                     const std::vector<MPImage> &srcs, const std::vector<MPImage> &dsts);
+
+static MPStatus mp_add_gauss(MPTables &T, std::vector<MPLaunch> &launches, const std::vector<Seg> &sgs,
+                             const std::vector<MPImage> &srcs, const std::vector<MPImage> &dsts)
+{
+    std::vector<size_t> ord(sgs.size());
+    for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) {
+        return (int)ceil(3.0 * sgs[a].core_p[0]) < (int)ceil(3.0 * sgs[b].core_p[0]);
+    });
+    std::vector<Seg> s2;
+    std::vector<MPImage> i2, o2;
+    for (size_t i : ord) {
+        s2.push_back(sgs[i]);
+        i2.push_back(srcs[i]);
+        o2.push_back(dsts[i]);
+    }
+    return mp_add_gauss_ordered(T, launches, s2, i2, o2);
+}
+
+static MPStatus mp_add_gauss_ordered(MPTables &T, std::vector<MPLaunch> &launches, const std::vector<Seg> &sgs,
+                                     const std::vector<MPImage> &srcs, const std::vector<MPImage> &dsts)
+{
+    if (sgs.empty()) return MILLIPYDE_SUCCESS;
+    const Seg &s0 = sgs[0];
+    double bytes = 0.0;
+    int rmax = 1;
+    bool vh = true, gs = true;
+    long long vh_rows = 0, gs_rows = 0;
+    const int code = mp_vh_code(s0.cin, s0.cmid), cm = code > 4 ? s0.cmid : 1;
+    for (size_t i = 0; i < sgs.size(); ++i) {
+        const int r = (int)ceil(3.0 * sgs[i].core_p[0]);
+        rmax = std::max(rmax, r);
+        vh = vh && mp_vh_ok(sgs[i], srcs[i]) && mp_vh_code(sgs[i].cin, sgs[i].cmid) == code;
+        gs = gs && mp_stream_ok(sgs[i], srcs[i]);
+        bytes += 4.0 * ((double)srcs[i].height * srcs[i].width * srcs[i].channels +
+                        (double)dsts[i].height * dsts[i].width * dsts[i].channels);
+        const int sw = mp_vh_fit_strip(std::min(r, MP_VH_RMAX), srcs[i].width, cm);
+        vh_rows += (long long)((srcs[i].width * cm + sw - 1) / sw) * srcs[i].height;
+    }
+    MPStatus st;
+    int cps = 0;
+    if (vh && mp_vh_prepare(code, &cps) == MILLIPYDE_SUCCESS) {
+        const int grid = cps * mp_num_sms();
+        const int rs = mp_vh_rows(vh_rows, grid);
+        std::vector<MPJob> js(sgs.size());
+        for (size_t i = 0; i < sgs.size(); ++i) {
+            st = mp_fill_job_vh(js[i], sgs[i], srcs[i], dsts[i], rs);
+            if (st != MILLIPYDE_SUCCESS) return st;
+        }
+        const size_t nl = launches.size();
+        st = T.add(launches, MPK_VH, code, 0, js, bytes);
+        if (st == MILLIPYDE_SUCCESS && launches.size() > nl) launches.back().grid = grid;
+        return st;
+    }
+    cudaGetLastError();
+    GsGeom g;
+    int grid = 0;
+    if (gs && rmax <= MP_MAX_RADIUS && mp_stream_setup(s0.cin, s0.cmid, rmax, &g, &grid)) {
+        for (size_t i = 0; i < sgs.size(); ++i)
+            gs_rows += (long long)((srcs[i].width + g.SW - 1) / g.SW) * srcs[i].height;
+        const int rs = mp_stream_rows(gs_rows, grid);
+        std::vector<MPJob> js(sgs.size());
+        for (size_t i = 0; i < sgs.size(); ++i) {
+            st = mp_fill_job_stream(js[i], sgs[i], srcs[i], dsts[i], g.SW, rs);
+            if (st != MILLIPYDE_SUCCESS) return st;
+        }
+        const size_t nl = launches.size();
+        st = T.add(launches, MPK_GSTREAM, mp_variant(s0.cin, s0.cmid), (size_t)g.total + 128, js, bytes);
+        if (st == MILLIPYDE_SUCCESS && launches.size() > nl) {
+            launches.back().gs = g;
+            launches.back().grid = grid;
+        }
+        return st;
+    }
+    // tile kernel
+    int tw, th, cinm = 1, cmidm = 1, pro = 0;
+    for (const Seg &sg : sgs) {
+        cinm = std::max(cinm, sg.cin);
+        cmidm = std::max(cmidm, sg.cmid);
+        pro |= sg.pro.n > 0;
+    }
+    mp_gauss_tiles(rmax, cinm, cmidm, pro, &tw, &th);
+    const size_t smem = mp_gauss_smem_bytes(tw, th, rmax, cinm, cmidm, pro);
+    std::vector<MPJob> js(sgs.size());
+    for (size_t i = 0; i < sgs.size(); ++i) {
+        st = mp_fill_job(js[i], sgs[i], srcs[i], dsts[i], tw, th);
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    return T.add(launches, MPK_GAUSS, mp_variant(s0.cin, s0.cmid), smem, js, bytes);
+}
+
+// Job table upload plus the per-launch work counters of a plan.
+static MPStatus mp_plan_finish(MPPlanImpl *P, MPTables &T, cudaStream_t s)
+{
+    MPStatus st = T.upload(P, s);
+    if (st != MILLIPYDE_SUCCESS || P->launches.empty()) return st;
+    const size_t cb = P->launches.size() * sizeof(int);
+    st = mp_malloc_async((void **)&P->counters, cb, s);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    return mp_cuda_status(cudaMemsetAsync(P->counters, 0, cb, s));
 }
 
 static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage *in,
@@ -898,94 +1011,17 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 }
             }
             if (kind == MPK_GAUSS) {
-                // single-channel streaming kernel when every image of the launch can take it
-                bool ok = true;
-                long long strip_rows = 0;
-                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
-                    const Seg &sg = segs[ch.imgs[q]][k];
-                    const MPImage &src = (k == 0) ? in[ch.imgs[q]] : inter[q][k - 1];
-                    ok = mp_vh_ok(sg, src);
-                    const int sw = mp_vh_fit_strip((int)ceil(3.0 * sg.core_p[0]), src.width);
-                    strip_rows += (long long)((src.width + sw - 1) / sw) * src.height;
+                std::vector<Seg> sgs;
+                std::vector<MPImage> srcs, dsts;
+                for (size_t q = 0; q < ch.imgs.size(); ++q) {
+                    const int img = ch.imgs[q];
+                    sgs.push_back(segs[img][k]);
+                    srcs.push_back((k == 0) ? in[img] : inter[q][k - 1]);
+                    dsts.push_back((k + 1 == nseg) ? out[img] : inter[q][k]);
                 }
-                int cps = 0;
-                const int c0 = segs[ch.imgs[0]][k].cin;
-                if (ok && mp_vh_prepare(c0, &cps) == MILLIPYDE_SUCCESS) {
-                    const int grid = cps * mp_num_sms();
-                    const int rs = mp_vh_rows(strip_rows, grid);
-                    std::vector<MPJob> js;
-                    double bytes = 0.0;
-                    for (size_t q = 0; q < ch.imgs.size(); ++q) {
-                        const int img = ch.imgs[q];
-                        const MPImage &src = (k == 0) ? in[img] : inter[q][k - 1];
-                        const MPImage &dst = (k + 1 == nseg) ? out[img] : inter[q][k];
-                        MPJob J;
-                        st = mp_fill_job_vh(J, segs[img][k], src, dst, rs);
-                        if (st != MILLIPYDE_SUCCESS) return st;
-                        bytes += 4.0 * ((double)src.height * src.width * src.channels +
-                                        (double)dst.height * dst.width * dst.channels);
-                        js.push_back(J);
-                    }
-                    const size_t nl = P->launches.size();
-                    st = T.add(P->launches, MPK_VH, c0, 0, js, bytes);
-                    if (st != MILLIPYDE_SUCCESS) return st;
-                    if (P->launches.size() > nl) P->launches.back().grid = grid;
-                    continue;
-                }
-                cudaGetLastError();
-            }
-            if (kind == MPK_GAUSS) {
-                // streaming kernel when every image of the launch can take it
-                bool ok = true;
-                int srmax = 0;
-                long long strip_rows = 0;
-                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
-                    const Seg &sg = segs[ch.imgs[q]][k];
-                    const MPImage &src = (k == 0) ? in[ch.imgs[q]] : inter[q][k - 1];
-                    ok = mp_stream_ok(sg, src);
-                    srmax = std::max(srmax, (int)ceil(3.0 * sg.core_p[0]));
-                }
-                const Seg &s0 = segs[ch.imgs[0]][k];
-                GsGeom g;
-                int grid = 0;
-                if (ok && srmax <= MP_MAX_RADIUS && mp_stream_setup(s0.cin, s0.cmid, srmax, &g, &grid)) {
-                    for (int img : ch.imgs)
-                        strip_rows += (long long)((segs[img][k].win + g.SW - 1) / g.SW) * segs[img][k].hin;
-                    const int rs = mp_stream_rows(strip_rows, grid);
-                    std::vector<MPJob> js;
-                    double bytes = 0.0;
-                    for (size_t q = 0; q < ch.imgs.size(); ++q) {
-                        const int img = ch.imgs[q];
-                        const Seg &sg = segs[img][k];
-                        const MPImage &src = (k == 0) ? in[img] : inter[q][k - 1];
-                        const MPImage &dst = (k + 1 == nseg) ? out[img] : inter[q][k];
-                        MPJob J;
-                        st = mp_fill_job_stream(J, sg, src, dst, g.SW, rs);
-                        if (st != MILLIPYDE_SUCCESS) return st;
-                        bytes += 4.0 * ((double)src.height * src.width * src.channels +
-                                        (double)dst.height * dst.width * dst.channels);
-                        js.push_back(J);
-                    }
-                    const size_t nl = P->launches.size();
-                    st = T.add(P->launches, MPK_GSTREAM, mp_variant(s0.cin, s0.cmid), (size_t)g.total + 128, js,
-                               bytes);
-                    if (st != MILLIPYDE_SUCCESS) return st;
-                    if (P->launches.size() > nl) {
-                        P->launches.back().gs = g;
-                        P->launches.back().grid = grid;
-                    }
-                    continue;
-                }
-                int rmax = 0, cinm = 1, cmidm = 1, pro = 0;
-                for (int img : ch.imgs) {
-                    const Seg &sg = segs[img][k];
-                    rmax = std::max(rmax, (int)ceil(3.0 * sg.core_p[0]));
-                    cinm = std::max(cinm, sg.cin);
-                    cmidm = std::max(cmidm, sg.cmid);
-                    pro |= sg.pro.n > 0;
-                }
-                mp_gauss_tiles(rmax, cinm, cmidm, pro, &tw, &th);
-                smem = mp_gauss_smem_bytes(tw, th, rmax, cinm, cmidm, pro);
+                st = mp_add_gauss(T, P->launches, sgs, srcs, dsts);
+                if (st != MILLIPYDE_SUCCESS) return st;
+                continue;
             }
             std::vector<MPJob> js;
             double bytes = 0.0;
@@ -1005,15 +1041,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             if (st != MILLIPYDE_SUCCESS) return st;
         }
     }
-    st = T.upload(P, s);
-    if (st != MILLIPYDE_SUCCESS) return st;
-    if (!P->launches.empty()) {
-        const size_t cb = P->launches.size() * sizeof(int);
-        st = mp_malloc_async((void **)&P->counters, cb, s);
-        if (st != MILLIPYDE_SUCCESS) return st;
-        st = mp_cuda_status(cudaMemsetAsync(P->counters, 0, cb, s));
-    }
-    return st;
+    return mp_plan_finish(P, T, s);
 }
 
 static MPStatus mp_plan_launch_one(const MPPlanImpl *P, size_t idx, cudaStream_t s)
@@ -1768,10 +1796,23 @@ static void mp_gauss_taps(double sigma, int r, float *w, float *dw)
 
 #define MP_BWD_SCRATCH_BYTES (2048ull << 20)
 
+extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const double *params, const float *x,
+                                              const float *dy, float *dx, double *dparams, const int *param_mask,
+                                              int B, int H, int W, int C, void *stream);
+
 extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *params, const float *x,
                                        const float *dy, float *dx, double *dparams, int B, int H,
                                        int W, int C, void *stream)
 {
+    return mpk_chain_backward_masked(ops, nops, params, x, dy, dx, dparams, nullptr, B, H, W, C, stream);
+}
+
+extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const double *params, const float *x,
+                                              const float *dy, float *dx, double *dparams, const int *param_mask,
+                                              int B, int H, int W, int C, void *stream)
+{
+    // param_mask[k] != 0: the parameters of op k want a gradient (null: all ops)
+    auto wants = [&](int k) { return dparams && (!param_mask || param_mask[k] != 0); };
     if (B < 0 || (B > 0 && (!x || !dy || !dx || (nops > 0 && (!ops || !params)))))
         return MP_ERROR_INVALID_ARGS;
     std::vector<MPShape> sh;
@@ -1858,9 +1899,15 @@ extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *p
             size_t smem = 0;
             const int kind = seg_of(0, k).kind;
             if (kind == MPK_GAUSS) {
-                std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> items;
-                for (int q = 0; q < nb; ++q) items.push_back({seg_of(q, k), {a_img(q, k), a_img(q, k + 1)}});
-                st = gauss_launch(items, js, &smem);
+                std::vector<Seg> sgs;
+                std::vector<MPImage> srcs, dsts;
+                for (int q = 0; q < nb; ++q) {
+                    sgs.push_back(seg_of(q, k));
+                    srcs.push_back(a_img(q, k));
+                    dsts.push_back(a_img(q, k + 1));
+                }
+                st = mp_add_gauss(T, P.launches, sgs, srcs, dsts);
+                continue;
             } else {
                 for (int q = 0; q < nb && st == MILLIPYDE_SUCCESS; ++q) {
                     MPJob J;
@@ -1903,20 +1950,29 @@ extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *p
                     J.cin = sh[j].c;
                     J.aux = (const float *)go.data;
                     J.aux_pitch = go.pitch / 4;
-                    J.acc = dparams ? dparams + (size_t)(b0 + q) * nops * 3 : nullptr;
+                    bool any = false;
+                    for (int t = j; t <= k; ++t) any = any || wants(t);
+                    J.acc = any ? dparams + (size_t)(b0 + q) * nops * 3 : nullptr;
                     for (int t = j; t <= k; ++t) J.pw_slot[t - j] = t;
                     js.push_back(J);
                 }
                 if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_POINT_ADJ, 0, js);
             } else if (ops[k] == MP_OP_GAUSSIAN) {
-                // dx = blur(g)
-                std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> items;
-                for (int q = 0; q < nb; ++q) items.push_back({seg_of(q, k), {gout_img(q), gin_img(q)}});
+                // dx = blur(g) (the zero-padded gaussian is self-adjoint)
+                {
+                    std::vector<Seg> sgs;
+                    std::vector<MPImage> srcs, dsts;
+                    for (int q = 0; q < nb; ++q) {
+                        sgs.push_back(seg_of(q, k));
+                        srcs.push_back(gout_img(q));
+                        dsts.push_back(gin_img(q));
+                    }
+                    st = mp_add_gauss(T, P.launches, sgs, srcs, dsts);
+                }
                 size_t smem = 0;
-                st = gauss_launch(items, js, &smem);
-                if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_GAUSS, smem, js);
-                // d sigma = <g, (W' (x) W + W (x) W') a_k>: two dot-mode launches
-                for (int pass = 0; pass < 2 && dparams && st == MILLIPYDE_SUCCESS; ++pass) {
+                // d sigma = <g, (W' (x) W + W (x) W') a_k>: two dot-mode launches,
+                // only when sigma wants a gradient
+                for (int pass = 0; pass < 2 && wants(k) && st == MILLIPYDE_SUCCESS; ++pass) {
                     std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> it2;
                     for (int q = 0; q < nb; ++q) it2.push_back({seg_of(q, k), {a_img(q, k), gout_img(q)}});
                     std::vector<MPJob> jd;
@@ -1950,7 +2006,7 @@ extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *p
                     J.sth = (float)sin(th_r);
                     J.aux = (const float *)go.data;
                     J.aux_pitch = go.pitch / 4;
-                    J.acc = dparams ? dparams + ((size_t)(b0 + q) * nops + k) * 3 : nullptr;
+                    J.acc = wants(k) ? dparams + ((size_t)(b0 + q) * nops + k) * 3 : nullptr;
                     js.push_back(J);
                 }
                 if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_ROTATE_ADJ, 0, js);
@@ -1973,7 +2029,7 @@ extern "C" MPStatus mpk_chain_backward(const int *ops, int nops, const double *p
             cur = nxt;
             k = j - 1;
         }
-        if (st == MILLIPYDE_SUCCESS) st = T.upload(&P, s);
+        if (st == MILLIPYDE_SUCCESS) st = mp_plan_finish(&P, T, s);
         if (st == MILLIPYDE_SUCCESS) st = mp_plan_launch(&P, s);
         mp_plan_free(&P, s);
     }

@@ -1,5 +1,6 @@
-// mp_vh.cu -- host side of the single-channel streaming gaussian (kernels in
-// mp_vh_c1.cu, mp_vh_c3.cu, mp_vh_c4.cu; device code in mp_vh.cuh).
+// mp_vh.cu -- host side of the streaming gaussian of mp_vh.cuh: the
+// single-channel family (kernels in mp_vh_c1.cu, mp_vh_c3.cu, mp_vh_c4.cu)
+// and the channel-preserving family (mp_vc_c3.cu, mp_vc_c4.cu).
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -12,36 +13,55 @@
 MP_VH_DECL(mp_vh_c1)
 MP_VH_DECL(mp_vh_c3)
 MP_VH_DECL(mp_vh_c4)
+MP_VH_DECL(mp_vc_c3)
+MP_VH_DECL(mp_vc_c4)
 
-static const void *mp_vh_fn(int cin, bool single)
+int mp_vh_code(int cin, int cmid)
 {
-    switch (cin) {
+    if (cmid == 1 && (cin == 1 || cin == 3 || cin == 4)) return cin;
+    if (cmid == cin && (cin == 3 || cin == 4)) return 4 + cin;
+    return -1;
+}
+
+static int mp_vh_code_cin(int code) { return code > 4 ? code - 4 : code; }
+static int mp_vh_code_cm(int code) { return code > 4 ? code - 4 : 1; }
+
+static const void *mp_vh_fn(int code, bool single)
+{
+    switch (code) {
     case 1: return single ? (const void *)mp_vh_c1_single : (const void *)mp_vh_c1_batch;
     case 3: return single ? (const void *)mp_vh_c3_single : (const void *)mp_vh_c3_batch;
     case 4: return single ? (const void *)mp_vh_c4_single : (const void *)mp_vh_c4_batch;
+    case 7: return single ? (const void *)mp_vc_c3_single : (const void *)mp_vc_c3_batch;
+    case 8: return single ? (const void *)mp_vc_c4_single : (const void *)mp_vc_c4_batch;
     default: return nullptr;
     }
 }
 
-int mp_vh_strip(int radius) { return 2 * MP_VH_NT - 2 * ((radius + 3) & ~3); }
+int mp_vh_strip(int radius, int cm) { return 2 * MP_VH_NT - 2 * ((radius * cm + 3) & ~3); }
 
-// Strip width for an image of width w: the fewest strips of at most
-// mp_vh_strip(radius) columns, evened out and rounded up to 8.
-int mp_vh_fit_strip(int radius, int w)
+// Strip width in columns for an image of width w pixels (w * cm columns):
+// the fewest strips of at most mp_vh_strip(radius, cm) columns, evened out
+// and rounded up to 8.
+int mp_vh_fit_strip(int radius, int w, int cm)
 {
-    const int maxw = mp_vh_strip(radius);
-    const int n = (w + maxw - 1) / maxw;
-    const int sw = ((w + n - 1) / n + 7) & ~7;
+    const int maxw = mp_vh_strip(radius, cm);
+    const int wc = w * cm;
+    const int n = (wc + maxw - 1) / maxw;
+    const int sw = ((wc + n - 1) / n + 7) & ~7;
     return sw < 8 ? 8 : (sw > maxw ? maxw : sw);
 }
 
-size_t mp_vh_smem(int cin) { return (size_t)mp_vh::mp_vh_smem_floats(cin) * 4 + 128; }
+size_t mp_vh_smem(int code)
+{
+    return (size_t)mp_vh::mp_vh_smem_floats(mp_vh_code_cin(code), mp_vh_code_cm(code)) * 4 + 128;
+}
 
-MPStatus mp_vh_prepare(int cin, int *ctas_per_sm)
+MPStatus mp_vh_prepare(int code, int *ctas_per_sm)
 {
     static std::mutex mtx;
     static std::vector<std::pair<const void *, int>> done;
-    const void *fn = mp_vh_fn(cin, false);
+    const void *fn = mp_vh_fn(code, false);
     if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -53,40 +73,40 @@ MPStatus mp_vh_prepare(int cin, int *ctas_per_sm)
             if (d.first == fn && d.second == dev) have = true;
         if (!have) {
             for (int single = 0; single < 2; ++single) {
-                e = cudaFuncSetAttribute(mp_vh_fn(cin, single != 0), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)mp_vh_smem(cin));
+                e = cudaFuncSetAttribute(mp_vh_fn(code, single != 0), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)mp_vh_smem(code));
                 if (e != cudaSuccess) return mp_cuda_status(e);
             }
             done.push_back({fn, dev});
         }
     }
     int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, MP_VH_NT, mp_vh_smem(cin));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, MP_VH_NT, mp_vh_smem(code));
     if (e != cudaSuccess) return mp_cuda_status(e);
     if (n < 1) return MP_ERROR_TOO_LARGE;
     *ctas_per_sm = n;
     return MILLIPYDE_SUCCESS;
 }
 
-MPStatus mp_vh_launch(int cin, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
+MPStatus mp_vh_launch(int code, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
                       int *counter, cudaStream_t s)
 {
     if (total <= 0) return MILLIPYDE_SUCCESS;
-    const void *fn = mp_vh_fn(cin, false);
+    const void *fn = mp_vh_fn(code, false);
     if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
     if (grid > total) grid = total;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&total, (void *)&err, (void *)&counter};
-    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_VH_NT), args, mp_vh_smem(cin), s));
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_VH_NT), args, mp_vh_smem(code), s));
 }
 
-MPStatus mp_vh_launch_single(int cin, const MPJob &job, int grid, int *err, cudaStream_t s)
+MPStatus mp_vh_launch_single(int code, const MPJob &job, int grid, int *err, cudaStream_t s)
 {
     if (job.ntiles <= 0) return MILLIPYDE_SUCCESS;
-    const void *fn = mp_vh_fn(cin, true);
+    const void *fn = mp_vh_fn(code, true);
     if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
     if (grid > job.ntiles) grid = job.ntiles;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&job, (void *)&err};
-    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_VH_NT), args, mp_vh_smem(cin), s));
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_VH_NT), args, mp_vh_smem(code), s));
 }

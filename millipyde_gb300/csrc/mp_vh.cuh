@@ -1,17 +1,24 @@
-// mp_vh.cuh -- the single-channel separable gaussian as one streaming kernel
-// (sm_103a): vertical pass in registers, horizontal pass through a small
-// shared-memory tile.
+// mp_vh.cuh -- the separable gaussian as one streaming kernel (sm_103a):
+// vertical pass in registers, horizontal pass through a small shared-memory
+// tile.
 //
 // Same operator as the other gaussian kernels (zero-padded separable
 // correlation with normalised exp(-k^2 / 2 sigma^2) taps, radius
 // ceil(3 sigma); the reference's weights and padding are
-// src/millipyde_image.cpp:745-756 and :170-172, :218-221), for segments whose
-// channel count after the prologue is 1: an rgb2grey prologue on 3- or
-// 4-channel sources, or a 1-channel source with a pointwise prologue.
+// src/millipyde_image.cpp:745-756 and :170-172, :218-221).  Two families:
+//   CM = 1   segments whose channel count after the prologue is 1: an
+//            rgb2grey prologue on 3- or 4-channel sources, or a 1-channel
+//            source with a pointwise prologue.  A column is a pixel.
+//   CM = C   channel-preserving segments on C = 3 or 4 interleaved channels
+//            (per-channel prologue / epilogue, no rgb2grey).  A column is
+//            one float of the interleaved row: the vertical pass does not
+//            care which channel a float belongs to, and the horizontal taps
+//            step by C floats.
 //
-// A work item is a STRIP of at most 2*NT - 2*R4 output columns (R4 = R
-// rounded up to 4; the width is fitted to each image) by RS output rows.  Each thread owns two adjacent columns
-// of the strip plus its halo and walks down them:
+// A work item is a STRIP of at most 2*NT - 2*R4 output columns (R4 = R*CM
+// rounded up to 4; the width is fitted to each image) by RS output rows.
+// Each thread owns two adjacent columns of the strip plus its halo and
+// walks down them:
 //   load   one thread copies the source rows of the strip, 8 at a time, by
 //          TMA (one box of 64 pixels per warp) into a double-buffered
 //          staging area, the next 8 rows in flight while the current ones
@@ -88,27 +95,37 @@ __device__ __forceinline__ float2 prologue(const float *slot, bool in0, bool in1
 }
 
 // Shared memory of one CTA (floats): 2 mbarriers + taps (64 floats), two
-// horizontal tiles [2][VR][VW], two staging buffers [2][NW][VR][64*CIN].
-__host__ __device__ constexpr int mp_vh_smem_floats(int cin)
+// horizontal tiles [2][VR][VW], two staging buffers [2][NW][VR][64*PX]
+// (PX = floats staged per column: CIN when CM = 1, else 1).
+__host__ __device__ constexpr int mp_vh_smem_floats(int cin, int cm)
 {
-    return 64 + 64 + 2 * MP_VH_VR * MP_VH_VW + 2 * MP_VH_VR * 2 * MP_VH_NT * cin;
+    return 64 + 64 + 2 * MP_VH_VR * MP_VH_VW + 2 * MP_VH_VR * 2 * MP_VH_NT * (cm == 1 ? cin : 1);
+}
+
+// Channel of interleaved float column f (f may be negative: halo columns).
+template <int CM>
+__device__ __forceinline__ int chan_of(int f)
+{
+    const int c = f % CM;
+    return c < 0 ? c + CM : c;
 }
 
 // One strip item with compiled radius R.  The strip is J.tw output columns
 // wide (a multiple of 8, at most 2*NT - 2*R4); window rows are counted from
 // source row y0 - R8 (R8 = R rounded up to 4) so that every step of VR rows
 // is exactly one staged group.
-template <int CIN, int R>
+template <int CIN, int CM, int R>
 __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32_t &gcount, int *err)
 {
     constexpr int NT = MP_VH_NT, VR = MP_VH_VR, VW = MP_VH_VW, NW = NT / 32;
-    constexpr int NTAP = 2 * R + 1, R4 = (R + 3) & ~3, E = R4 - R;
-    constexpr int R8 = R4;                                // window row padding (2*R8 is a multiple of 8)
+    constexpr int NTAP = 2 * R + 1, RC = R * CM, R4 = (RC + 3) & ~3, E = R4 - RC;
+    constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
     constexpr int D = R8 - R;                             // tap offset inside the window
     constexpr int NWIN = VR + 2 * R8;
     constexpr int NPRE = 2 * R8 / VR;                     // groups holding the window head
-    constexpr int NLD = (E + 8 + 2 * R + 3) / 4;
-    constexpr int BOXW = 64 * CIN;                        // staged floats per warp and row
+    constexpr int NLD = (E + 8 + 2 * RC + 3) / 4;
+    constexpr int PX = CM == 1 ? CIN : 1;                 // staged floats per column
+    constexpr int BOXW = 64 * PX;                         // staged floats per warp and row
     constexpr int GF = NW * VR * BOXW;                    // staged floats per group
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
@@ -117,13 +134,14 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     float *stg = tile + 2 * VR * VW;                      // [2][NW][VR][BOXW]
 
     const int sy = lt / J.tiles_x, sx = lt - sy * J.tiles_x;
-    const int H = J.h, W = J.w;
+    const int H = J.h, W = J.w * CM;                      // W in columns
     const int swo = J.tw, ng = swo >> 3;
     const int x0 = sx * swo, y0 = sy * J.th;
     const int y1 = min(H, y0 + J.th);
     const int nsteps = (y1 - y0 + VR - 1) / VR;
     const int xv = x0 - R4 + 2 * tid;                     // this thread's first column
     const bool in0 = xv >= 0 && xv < W, in1 = xv + 1 >= 0 && xv + 1 < W;
+    const int ch0 = chan_of<CM>(xv), ch1 = chan_of<CM>(xv + 1);
     const int ybase = y0 - R8;                            // source row of window row 0
 
     __syncthreads();   // the previous item is done with the taps, tiles and staging
@@ -131,6 +149,11 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     const PwFast pro = mp_pw_fast(J.pro);
     const bool grey_only = J.pro.n == 1 && pro.op == MP_OP_RGB2GREY;
     const PwFast epi = mp_pw_fast(J.epi);
+    PwRegs pro3, epi3;   // the channel-preserving family's lists in registers
+    if constexpr (CM > 1) {
+        pro3 = mp_pw_regs(J.pro);
+        epi3 = mp_pw_regs(J.epi);
+    }
     const int flip = J.flip, wo = J.wo, dp = J.dst_pitch;
     const bool vec = !flip && J.vec_out;
     float *const dst = J.dst;
@@ -144,7 +167,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
         float *b = stg + (G & 1u) * GF;
         mp_mbar_arrive_expect_tx(bar, (uint32_t)(GF * 4));
         for (int w = 0; w < NW; ++w)
-            mp_tma_load_2d(b + w * VR * BOXW, &J.tmap, bar, (x0 - R4 + 64 * w) * CIN, ybase + VR * g);
+            mp_tma_load_2d(b + w * VR * BOXW, &J.tmap, bar, (x0 - R4 + 64 * w) * PX, ybase + VR * g);
     };
     // all threads: wait for group g; false after a timeout (error word set)
     auto wait = [&](int g) -> bool {
@@ -158,9 +181,33 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     // win[w0 .. w0 + VR): the prologue kind is decided once per group
     auto group_values = [&](int g, float2 *wdst) {
         const uint32_t G = g0 + (uint32_t)g;
-        const float *slot = stg + (G & 1u) * GF + warp * VR * BOXW + lane * 2 * CIN;
+        const float *slot = stg + (G & 1u) * GF + warp * VR * BOXW + lane * 2 * PX;
         const int yr = ybase + VR * g;
-        if (CIN >= 3 && grey_only) {
+        if constexpr (CM > 1) {
+            // interleaved floats: per-channel prologue on each column
+            if (J.pro.n) {
+                float v[2 * VR];
+                int chv[2 * VR];
+#pragma unroll
+                for (int j = 0; j < VR; ++j) {
+                    const float2 t = *reinterpret_cast<const float2 *>(slot + j * BOXW);
+                    v[2 * j] = t.x;
+                    v[2 * j + 1] = t.y;
+                    chv[2 * j] = ch0;
+                    chv[2 * j + 1] = ch1;
+                }
+                mp_pw_chan_n<2 * VR>(pro3, J.pro, v, chv, CM);
+#pragma unroll
+                for (int j = 0; j < VR; ++j) {
+                    const bool rin = (unsigned)(yr + j) < (unsigned)H;
+                    wdst[j] = make_float2(in0 && rin ? v[2 * j] : 0.f, in1 && rin ? v[2 * j + 1] : 0.f);
+                }
+            } else {
+                // no prologue: the copy's zero fill already pads the image
+#pragma unroll
+                for (int j = 0; j < VR; ++j) wdst[j] = *reinterpret_cast<const float2 *>(slot + j * BOXW);
+            }
+        } else if (CIN >= 3 && grey_only) {
 #pragma unroll
             for (int j = 0; j < VR; ++j) {
                 const bool rin = (unsigned)(yr + j) < (unsigned)H;
@@ -223,38 +270,81 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                 const int xo0 = x0 + 8 * g;
                 if (y >= y1 || xo0 >= W) continue;
                 const float *gp = tr + rr * VW + 8 * g;
-                float x[4 * NLD];
-#pragma unroll
-                for (int q = 0; q < NLD; ++q) {
-                    const float4 v = ld4(gp + 4 * q);
-                    x[4 * q] = v.x;
-                    x[4 * q + 1] = v.y;
-                    x[4 * q + 2] = v.z;
-                    x[4 * q + 3] = v.w;
-                }
                 float o[8];
+                if constexpr (CM == 1) {
+                    float x[4 * NLD];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    float a0 = 0.f, a1 = 0.f;
-#pragma unroll
-                    for (int m = 0; m < NTAP; ++m) {
-                        if (m & 1) a1 = fmaf(w2[m].x, x[E + k + m], a1);
-                        else a0 = fmaf(w2[m].x, x[E + k + m], a0);
+                    for (int q = 0; q < NLD; ++q) {
+                        const float4 v = ld4(gp + 4 * q);
+                        x[4 * q] = v.x;
+                        x[4 * q + 1] = v.y;
+                        x[4 * q + 2] = v.z;
+                        x[4 * q + 3] = v.w;
                     }
-                    o[k] = a0 + a1;
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+                        for (int m = 0; m < NTAP; ++m) {
+                            if (m & 1) a1 = fmaf(w2[m].x, x[E + k + m], a1);
+                            else a0 = fmaf(w2[m].x, x[E + k + m], a0);
+                        }
+                        o[k] = a0 + a1;
+                    }
+                } else {
+                    // taps CM floats apart: consume the tile row in order so
+                    // that only the 8 sums stay live (tap order per output)
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) o[k] = 0.f;
+#pragma unroll
+                    for (int q = 0; q < NLD; ++q) {
+                        const float4 v = ld4(gp + 4 * q);
+                        const float e4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                const int t = 4 * q + u - E - k;   // = m * CM for tap m
+                                if (t >= 0 && t % CM == 0 && t / CM < NTAP) o[k] = fmaf(w2[t / CM].x, e4[u], o[k]);
+                            }
+                        }
+                    }
                 }
                 if (epi.n) {
+                    if constexpr (CM == 1) {
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) o[k] = mp_pw_chan_f(epi, J.epi, o[k], 0, 1);
+                        for (int k = 0; k < 8; ++k) o[k] = mp_pw_chan_f(epi, J.epi, o[k], 0, 1);
+                    } else {
+                        const int cb = xo0 % CM;
+                        int chv[8];
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) chv[k] = (cb + k) % CM;
+                        mp_pw_chan_n<8>(epi3, J.epi, o, chv, CM);
+                    }
                 }
                 float *drow = dst + (size_t)y * dp;
                 if (vec && xo0 + 8 <= W) {
                     *reinterpret_cast<float4 *>(drow + xo0) = make_float4(o[0], o[1], o[2], o[3]);
                     *reinterpret_cast<float4 *>(drow + xo0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
-                } else {
+                } else if constexpr (CM == 1) {
 #pragma unroll
                     for (int k = 0; k < 8; ++k)
                         if (xo0 + k < W) drow[flip ? wo - 1 - (xo0 + k) : xo0 + k] = o[k];
+                } else if (CM == 4 && flip && J.vec_out && xo0 + 8 <= W) {
+                    // two whole pixels, mirrored: one float4 each
+                    const int px = xo0 >> 2;
+                    *reinterpret_cast<float4 *>(drow + (wo - 1 - px) * 4) = make_float4(o[0], o[1], o[2], o[3]);
+                    *reinterpret_cast<float4 *>(drow + (wo - 2 - px) * 4) = make_float4(o[4], o[5], o[6], o[7]);
+                } else {
+                    // fliplr mirrors pixels and keeps the channel order
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const int f = xo0 + k;
+                        if (f < W) {
+                            const int px = f / CM, c = f - px * CM;
+                            drow[flip ? (wo - 1 - px) * CM + c : f] = o[k];
+                        }
+                    }
                 }
             }
         }
@@ -272,12 +362,12 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     gcount = g0 + (uint32_t)ngroups;
 }
 
-template <int CIN>
+template <int CIN, int CM>
 __device__ __forceinline__ void vh_dispatch(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
 {
     switch (J.radius) {
 #define MP_VH_CASE(RR) \
-    case RR: vh_item<CIN, RR>(J, lt, smem, gc, err); break;
+    case RR: vh_item<CIN, CM, RR>(J, lt, smem, gc, err); break;
         MP_VH_CASE(1) MP_VH_CASE(2) MP_VH_CASE(3) MP_VH_CASE(4) MP_VH_CASE(5) MP_VH_CASE(6)
         MP_VH_CASE(7) MP_VH_CASE(8) MP_VH_CASE(9) MP_VH_CASE(10) MP_VH_CASE(11) MP_VH_CASE(12)
 #undef MP_VH_CASE
@@ -305,7 +395,7 @@ __device__ __forceinline__ void vh_init(float *smem)
 }  // namespace mp_vh
 
 // Persistent kernels: CTA b takes strip items b, b + grid, ...
-#define MP_VH_KERNELS(NAME, CIN)                                                                     \
+#define MP_VH_KERNELS(NAME, CIN, CM)                                                                   \
     __global__ void __launch_bounds__(MP_VH_NT, 3) NAME##_batch(                                    \
         const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int total, int *err,      \
         int *counter)                                                                               \
@@ -318,7 +408,7 @@ __device__ __forceinline__ void vh_init(float *smem)
         /* first item by CTA index, the rest from the launch's counter */                          \
         for (int t = blockIdx.x; t < total;) {                                                      \
             const MPJob &J = jobs[__ldg(tile_job + t)];                                             \
-            mp_vh::vh_dispatch<CIN>(J, t - J.tile0, smem, gc, err);                                 \
+            mp_vh::vh_dispatch<CIN, CM>(J, t - J.tile0, smem, gc, err);                                 \
             __syncthreads(); /* every thread has read next_item */                                  \
             if (threadIdx.x == 0) next_item = (int)gridDim.x + atomicAdd(counter, 1);              \
             __syncthreads();                                                                        \
@@ -333,5 +423,5 @@ __device__ __forceinline__ void vh_init(float *smem)
         mp_vh::vh_init(smem);                                                                       \
         uint32_t gc = 0;                                                                            \
         for (int t = blockIdx.x; t < job.ntiles; t += gridDim.x)                                    \
-            mp_vh::vh_dispatch<CIN>(job, t, smem, gc, err);                                         \
+            mp_vh::vh_dispatch<CIN, CM>(job, t, smem, gc, err);                                         \
     }

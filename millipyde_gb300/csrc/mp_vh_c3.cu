@@ -3,4 +3,4 @@
 // so the per-radius instances compile in parallel.
 #include "mp_vh.cuh"
 
-MP_VH_KERNELS(mp_vh_c3, 3)
+MP_VH_KERNELS(mp_vh_c3, 3, 1)

@@ -3,4 +3,4 @@
 // so the per-radius instances compile in parallel.
 #include "mp_vh.cuh"
 
-MP_VH_KERNELS(mp_vh_c4, 4)
+MP_VH_KERNELS(mp_vh_c4, 4, 1)

@@ -169,6 +169,19 @@ def test_pointwise_before_gaussian_keeps_zero_padding(gpu, rng):
     check_spec(spec, xs)
 
 
+def test_channel_preserving_gaussian_strips_and_mirror(gpu, rng):
+    # RGB / RGBA blur across several strips, a per-channel prologue and
+    # epilogue, a mirrored output, radii inside (2, 4, 12) and beyond (14)
+    # the compiled range
+    for c in (3, 4):
+        for sigma in (0.4, 1.3, 4.0, 4.4):
+            spec = [dict(op="colorize", lo=(1.2, 0.7, 0.9)), dict(op="gaussian", lo=(sigma,)),
+                    dict(op="adjust_gamma", lo=(0.8, 1.0)), dict(op="fliplr")]
+            xs = [rng.random((70, 301, c), dtype=np.float32), rng.random((9, 5, c), dtype=np.float32)]
+            check_spec(spec, xs)
+            check_spec(spec[1:2], xs[:1])
+
+
 def test_chunking_over_l2_budget(gpu, rng):
     spec = [dict(op="rgb2grey"), dict(op="gaussian", lo=(2.0,)), dict(op="rotate", lo=(10.0,))]
     xs = [rng.random((640, 640, 3), dtype=np.float32) for _ in range(40)]   # > 48 MB of intermediates
