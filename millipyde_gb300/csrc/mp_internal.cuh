@@ -32,6 +32,7 @@ enum MPKind {
     MPK_VH = 8
 };
 #define MP_VH_RMAX 12
+#define MP_VH_RBIG 24   // largest bucket radius of the mp_vh.cuh kernels
 
 
 // Output tile of the footprint-staged rotate per channel count.
@@ -444,13 +445,16 @@ MPStatus mp_ro_launch(int c, const MPJob *jobs_dev, const int *tile_job, int tot
                       int *err, cudaStream_t s);
 MPStatus mp_ro_launch_single(int c, const MPJob &job, int buf_floats, int grid, int *err, cudaStream_t s);
 size_t mp_ro_smem(int buf_floats);
-// Streaming gaussian of mp_vh.cuh (mp_vh*.cu, mp_vc*.cu).  A kernel code
-// names the family: the source channel count (1, 3, 4) for the
+// Streaming gaussian of mp_vh.cuh (mp_vh*.cu, mp_vc*.cu, mp_vb*.cu).  A
+// kernel code names the family: the source channel count (1, 3, 4) for the
 // single-channel family (cmid 1), 4 + C (7, 8) for the channel-preserving
-// family on C = 3 or 4 interleaved channels; -1 if neither takes
-// (cin, cmid).  Strips are counted in columns: pixels when cm = 1, floats of
-// the interleaved row otherwise.
-int mp_vh_code(int cin, int cmid);
+// family on C = 3 or 4 interleaved channels, plus 16 for the radius buckets
+// above MP_VH_RMAX (1-channel sources, RGB and RGBA only); -1 if no kernel
+// takes (cin, cmid, radius).  mp_vh_bucket is the radius a job runs with
+// (its strip halo).  Strips are counted in columns: pixels when cm = 1,
+// floats of the interleaved row otherwise.
+int mp_vh_code(int cin, int cmid, int radius);
+int mp_vh_bucket(int radius);
 int mp_vh_strip(int radius, int cm);
 int mp_vh_fit_strip(int radius, int w, int cm);
 MPStatus mp_vh_prepare(int code, int *ctas_per_sm);

@@ -685,9 +685,8 @@ struct MPTables {
 // its source rows are TMA-legal.
 static bool mp_vh_ok(const Seg &sg, const MPImage &in)
 {
-    if (sg.kind != MPK_GAUSS || mp_vh_code(sg.cin, sg.cmid) < 0 || sg.cout != sg.cmid) return false;
     const int r = (int)ceil(3.0 * sg.core_p[0]);
-    if (r < 1 || r > MP_VH_RMAX) return false;
+    if (sg.kind != MPK_GAUSS || mp_vh_code(sg.cin, sg.cmid, r) < 0 || sg.cout != sg.cmid) return false;
     for (int i = 0; i < sg.epi.n; ++i)
         if (sg.epi.op[i].op == MP_OP_RGB2GREY) return false;
     return (in.pitch % 16) == 0 && ((uintptr_t)in.data % 16) == 0 && in.width > 0 && in.height > 0 &&
@@ -698,8 +697,8 @@ static MPStatus mp_fill_job_vh(MPJob &J, const Seg &sg, const MPImage &in, const
 {
     MPStatus st = mp_fill_job(J, sg, in, out, 8, 8);   // radius, taps, pro/epilogue, flip
     if (st != MILLIPYDE_SUCCESS) return st;
-    const int cm = mp_vh_code(sg.cin, sg.cmid) > 4 ? sg.cmid : 1;   // channels per pixel column
-    const int sw = mp_vh_fit_strip(J.radius, in.width, cm);           // in columns
+    const int cm = (mp_vh_code(sg.cin, sg.cmid, J.radius) & 15) > 4 ? sg.cmid : 1;   // channels per column
+    const int sw = mp_vh_fit_strip(mp_vh_bucket(J.radius), in.width, cm);           // in columns
     J.tw = sw;
     J.th = rs;
     J.tiles_x = (in.width * cm + sw - 1) / sw;
@@ -736,15 +735,15 @@ static MPStatus mp_vh_run_single(const Seg &sg, const MPImage &in, const MPImage
 {
     *used = false;
     if (!mp_vh_ok(sg, in)) return MILLIPYDE_SUCCESS;
-    const int code = mp_vh_code(sg.cin, sg.cmid), cm = code > 4 ? sg.cmid : 1;
+    const int r = (int)ceil(3.0 * sg.core_p[0]);
+    const int code = mp_vh_code(sg.cin, sg.cmid, r), cm = (code & 15) > 4 ? sg.cmid : 1;
     int cps = 0;
     if (mp_vh_prepare(code, &cps) != MILLIPYDE_SUCCESS) {
         cudaGetLastError();
         return MILLIPYDE_SUCCESS;
     }
     const int grid = cps * mp_num_sms();
-    const int r = (int)ceil(3.0 * sg.core_p[0]);
-    const int sw = mp_vh_fit_strip(r, in.width, cm);
+    const int sw = mp_vh_fit_strip(mp_vh_bucket(r), in.width, cm);
     MPJob J;
     MPStatus st = mp_fill_job_vh(J, sg, in, out,
                                  mp_vh_rows((long long)((in.width * cm + sw - 1) / sw) * in.height, grid));
@@ -789,35 +788,59 @@ static MPStatus mp_add_gauss_ordered(MPTables &T, std::vector<MPLaunch> &launche
 {
     if (sgs.empty()) return MILLIPYDE_SUCCESS;
     const Seg &s0 = sgs[0];
+    const size_t n = sgs.size();
     double bytes = 0.0;
     int rmax = 1;
     bool vh = true, gs = true;
-    long long vh_rows = 0, gs_rows = 0;
-    const int code = mp_vh_code(s0.cin, s0.cmid), cm = code > 4 ? s0.cmid : 1;
-    for (size_t i = 0; i < sgs.size(); ++i) {
+    long long gs_rows = 0;
+    std::vector<int> code(n);
+    for (size_t i = 0; i < n; ++i) {
         const int r = (int)ceil(3.0 * sgs[i].core_p[0]);
         rmax = std::max(rmax, r);
-        vh = vh && mp_vh_ok(sgs[i], srcs[i]) && mp_vh_code(sgs[i].cin, sgs[i].cmid) == code;
+        code[i] = mp_vh_code(sgs[i].cin, sgs[i].cmid, r);
+        vh = vh && mp_vh_ok(sgs[i], srcs[i]);
         gs = gs && mp_stream_ok(sgs[i], srcs[i]);
         bytes += 4.0 * ((double)srcs[i].height * srcs[i].width * srcs[i].channels +
                         (double)dsts[i].height * dsts[i].width * dsts[i].channels);
-        const int sw = mp_vh_fit_strip(std::min(r, MP_VH_RMAX), srcs[i].width, cm);
-        vh_rows += (long long)((srcs[i].width * cm + sw - 1) / sw) * srcs[i].height;
     }
     MPStatus st;
-    int cps = 0;
-    if (vh && mp_vh_prepare(code, &cps) == MILLIPYDE_SUCCESS) {
-        const int grid = cps * mp_num_sms();
-        const int rs = mp_vh_rows(vh_rows, grid);
-        std::vector<MPJob> js(sgs.size());
-        for (size_t i = 0; i < sgs.size(); ++i) {
-            st = mp_fill_job_vh(js[i], sgs[i], srcs[i], dsts[i], rs);
+    // mp_vh.cuh kernels: one launch per kernel code (radius order keeps each
+    // code's images together); every code is prepared before any is added
+    std::vector<std::pair<size_t, size_t>> runs;
+    std::vector<int> grids;
+    for (size_t a = 0; vh && a < n;) {
+        size_t b = a + 1;
+        while (b < n && code[b] == code[a]) ++b;
+        int cps = 0;
+        if (mp_vh_prepare(code[a], &cps) != MILLIPYDE_SUCCESS) vh = false;
+        runs.push_back({a, b});
+        grids.push_back(cps * mp_num_sms());
+        a = b;
+    }
+    if (vh) {
+        for (size_t q = 0; q < runs.size(); ++q) {
+            const size_t a = runs[q].first, b = runs[q].second;
+            const int cm = (code[a] & 15) > 4 ? sgs[a].cmid : 1;
+            long long vh_rows = 0;
+            double rb = 0.0;
+            for (size_t i = a; i < b; ++i) {
+                const int sw = mp_vh_fit_strip(mp_vh_bucket((int)ceil(3.0 * sgs[i].core_p[0])), srcs[i].width, cm);
+                vh_rows += (long long)((srcs[i].width * cm + sw - 1) / sw) * srcs[i].height;
+                rb += 4.0 * ((double)srcs[i].height * srcs[i].width * srcs[i].channels +
+                             (double)dsts[i].height * dsts[i].width * dsts[i].channels);
+            }
+            const int rs = mp_vh_rows(vh_rows, grids[q]);
+            std::vector<MPJob> js(b - a);
+            for (size_t i = a; i < b; ++i) {
+                st = mp_fill_job_vh(js[i - a], sgs[i], srcs[i], dsts[i], rs);
+                if (st != MILLIPYDE_SUCCESS) return st;
+            }
+            const size_t nl = launches.size();
+            st = T.add(launches, MPK_VH, code[a], 0, js, rb);
             if (st != MILLIPYDE_SUCCESS) return st;
+            if (launches.size() > nl) launches.back().grid = grids[q];
         }
-        const size_t nl = launches.size();
-        st = T.add(launches, MPK_VH, code, 0, js, bytes);
-        if (st == MILLIPYDE_SUCCESS && launches.size() > nl) launches.back().grid = grid;
-        return st;
+        return MILLIPYDE_SUCCESS;
     }
     cudaGetLastError();
     GsGeom g;

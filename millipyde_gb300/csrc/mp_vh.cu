@@ -1,6 +1,7 @@
 // mp_vh.cu -- host side of the streaming gaussian of mp_vh.cuh: the
-// single-channel family (kernels in mp_vh_c1.cu, mp_vh_c3.cu, mp_vh_c4.cu)
-// and the channel-preserving family (mp_vc_c3.cu, mp_vc_c4.cu).
+// single-channel family (kernels in mp_vh_c1.cu, mp_vh_c3.cu, mp_vh_c4.cu),
+// the channel-preserving family (mp_vc_c3.cu, mp_vc_c4.cu) and the
+// radius buckets above 12 of the channel-keeping kernels (mp_vb_c*.cu).
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -15,16 +16,25 @@ MP_VH_DECL(mp_vh_c3)
 MP_VH_DECL(mp_vh_c4)
 MP_VH_DECL(mp_vc_c3)
 MP_VH_DECL(mp_vc_c4)
+MP_VH_DECL(mp_vb_c1)
+MP_VH_DECL(mp_vb_c3)
+MP_VH_DECL(mp_vb_c4)
 
-int mp_vh_code(int cin, int cmid)
+int mp_vh_code(int cin, int cmid, int radius)
 {
-    if (cmid == 1 && (cin == 1 || cin == 3 || cin == 4)) return cin;
-    if (cmid == cin && (cin == 3 || cin == 4)) return 4 + cin;
-    return -1;
+    int code = -1;
+    if (cmid == 1 && (cin == 1 || cin == 3 || cin == 4)) code = cin;
+    else if (cmid == cin && (cin == 3 || cin == 4)) code = 4 + cin;
+    if (code < 0 || radius < 1 || radius > MP_VH_RBIG) return -1;
+    if (radius <= MP_VH_RMAX) return code;
+    // buckets: channel-keeping kernels only (1-channel source, RGB, RGBA)
+    return (code == 1 || code == 7 || code == 8) ? code + 16 : -1;
 }
 
-static int mp_vh_code_cin(int code) { return code > 4 ? code - 4 : code; }
-static int mp_vh_code_cm(int code) { return code > 4 ? code - 4 : 1; }
+int mp_vh_bucket(int radius) { return radius <= MP_VH_RMAX ? radius : (radius <= 16 ? 16 : (radius <= 20 ? 20 : 24)); }
+
+static int mp_vh_code_cin(int code) { code &= 15; return code > 4 ? code - 4 : code; }
+static int mp_vh_code_cm(int code) { code &= 15; return code > 4 ? code - 4 : 1; }
 
 static const void *mp_vh_fn(int code, bool single)
 {
@@ -34,6 +44,9 @@ static const void *mp_vh_fn(int code, bool single)
     case 4: return single ? (const void *)mp_vh_c4_single : (const void *)mp_vh_c4_batch;
     case 7: return single ? (const void *)mp_vc_c3_single : (const void *)mp_vc_c3_batch;
     case 8: return single ? (const void *)mp_vc_c4_single : (const void *)mp_vc_c4_batch;
+    case 17: return single ? (const void *)mp_vb_c1_single : (const void *)mp_vb_c1_batch;
+    case 23: return single ? (const void *)mp_vb_c3_single : (const void *)mp_vb_c3_batch;
+    case 24: return single ? (const void *)mp_vb_c4_single : (const void *)mp_vb_c4_batch;
     default: return nullptr;
     }
 }

@@ -53,6 +53,16 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
     return *reinterpret_cast<float2 *>(&d);
 }
 
+// d = a + b on float pairs.
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<unsigned long long *>(&a)), "l"(*reinterpret_cast<unsigned long long *>(&b)));
+    return *reinterpret_cast<float2 *>(&d);
+}
+
 // Prologue of the two staged pixels -> one value each; in0 / in1 say
 // whether each pixel lies inside the image (zero otherwise, after the
 // prologue: the zero padding of the blur).
@@ -114,11 +124,18 @@ __device__ __forceinline__ int chan_of(int f)
 // wide (a multiple of 8, at most 2*NT - 2*R4); window rows are counted from
 // source row y0 - R8 (R8 = R rounded up to 4) so that every step of VR rows
 // is exactly one staged group.
+// Radii above MP_VH_RMAX are buckets: a job of radius r <= R runs with its
+// taps centred in 2R + 1 (zeros outside), the vertical pass adds the two
+// window rows of each symmetric tap pair before multiplying (R + 1 tap
+// registers instead of 2R + 1) and the horizontal pass consumes the tile row
+// in order.
 template <int CIN, int CM, int R>
 __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32_t &gcount, int *err)
 {
+    constexpr bool BIG = R > MP_VH_RMAX;
     constexpr int NT = MP_VH_NT, VR = MP_VH_VR, VW = MP_VH_VW, NW = NT / 32;
     constexpr int NTAP = 2 * R + 1, RC = R * CM, R4 = (RC + 3) & ~3, E = R4 - RC;
+    constexpr int NW2 = BIG ? R + 1 : NTAP;               // tap registers
     constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
     constexpr int D = R8 - R;                             // tap offset inside the window
     constexpr int NWIN = VR + 2 * R8;
@@ -145,7 +162,12 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     const int ybase = y0 - R8;                            // source row of window row 0
 
     __syncthreads();   // the previous item is done with the taps, tiles and staging
-    if (tid < 64) taps[tid] = tid < NTAP ? J.wts[tid] : 0.f;
+    if constexpr (BIG) {
+        const int sh = R - J.radius;                      // bucket shift of the job's taps
+        if (tid < 64) taps[tid] = (tid >= sh && tid < NTAP - sh) ? J.wts[tid - sh] : 0.f;
+    } else {
+        if (tid < 64) taps[tid] = tid < NTAP ? J.wts[tid] : 0.f;
+    }
     const PwFast pro = mp_pw_fast(J.pro);
     const bool grey_only = J.pro.n == 1 && pro.op == MP_OP_RGB2GREY;
     const PwFast epi = mp_pw_fast(J.epi);
@@ -227,9 +249,11 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
         issue(0);
     }
     __syncthreads();
-    float2 w2[NTAP];
+    float2 w2[NW2];
 #pragma unroll
-    for (int m = 0; m < NTAP; ++m) w2[m] = make_float2(taps[m], taps[m]);
+    for (int m = 0; m < NW2; ++m) w2[m] = make_float2(taps[m], taps[m]);
+    // tap m of 2R + 1 (symmetric storage for the buckets)
+    auto tap = [&](int m) -> float { return BIG ? w2[m <= R ? m : 2 * R - m].x : w2[m].x; };
 
     float2 win[NWIN];
     bool alive = true;
@@ -254,7 +278,14 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
             for (int o = 0; o < VR; ++o) {
                 float2 a = make_float2(0.f, 0.f);
 #pragma unroll
-                for (int k = 0; k < NTAP; ++k) a = fma2(w2[k], win[o + D + k], a);
+                if constexpr (BIG) {
+                    a = fma2(w2[R], win[o + D + R], a);
+#pragma unroll
+                    for (int k = 0; k < R; ++k) a = fma2(w2[k], add2(win[o + D + k], win[o + D + 2 * R - k]), a);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < NTAP; ++k) a = fma2(w2[k], win[o + D + k], a);
+                }
                 *reinterpret_cast<float2 *>(tb + o * VW) = a;
             }
 #pragma unroll
@@ -271,7 +302,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                 if (y >= y1 || xo0 >= W) continue;
                 const float *gp = tr + rr * VW + 8 * g;
                 float o[8];
-                if constexpr (CM == 1) {
+                if constexpr (CM == 1 && !BIG) {
                     float x[4 * NLD];
 #pragma unroll
                     for (int q = 0; q < NLD; ++q) {
@@ -305,7 +336,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
 #pragma unroll
                             for (int k = 0; k < 8; ++k) {
                                 const int t = 4 * q + u - E - k;   // = m * CM for tap m
-                                if (t >= 0 && t % CM == 0 && t / CM < NTAP) o[k] = fmaf(w2[t / CM].x, e4[u], o[k]);
+                                if (t >= 0 && t % CM == 0 && t / CM < NTAP) o[k] = fmaf(tap(t / CM), e4[u], o[k]);
                             }
                         }
                     }
@@ -375,6 +406,15 @@ __device__ __forceinline__ void vh_dispatch(const MPJob &J, int lt, float *smem,
     }
 }
 
+// Radii above MP_VH_RMAX, rounded up to a bucket.
+template <int CIN, int CM>
+__device__ __forceinline__ void vh_dispatch_big(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
+{
+    if (J.radius <= 16) vh_item<CIN, CM, 16>(J, lt, smem, gc, err);
+    else if (J.radius <= 20) vh_item<CIN, CM, 20>(J, lt, smem, gc, err);
+    else if (J.radius <= MP_VH_RBIG) vh_item<CIN, CM, MP_VH_RBIG>(J, lt, smem, gc, err);
+}
+
 __device__ __forceinline__ float *vh_base(float4 *raw)
 {
     unsigned char *p = reinterpret_cast<unsigned char *>(raw);
@@ -395,8 +435,8 @@ __device__ __forceinline__ void vh_init(float *smem)
 }  // namespace mp_vh
 
 // Persistent kernels: CTA b takes strip items b, b + grid, ...
-#define MP_VH_KERNELS(NAME, CIN, CM)                                                                   \
-    __global__ void __launch_bounds__(MP_VH_NT, 3) NAME##_batch(                                    \
+#define MP_VH_KERNELS_X(NAME, CIN, CM, DISPATCH, MINB)                                                                 \
+    __global__ void __launch_bounds__(MP_VH_NT, MINB) NAME##_batch(                                    \
         const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int total, int *err,      \
         int *counter)                                                                               \
     {                                                                                               \
@@ -408,14 +448,14 @@ __device__ __forceinline__ void vh_init(float *smem)
         /* first item by CTA index, the rest from the launch's counter */                          \
         for (int t = blockIdx.x; t < total;) {                                                      \
             const MPJob &J = jobs[__ldg(tile_job + t)];                                             \
-            mp_vh::vh_dispatch<CIN, CM>(J, t - J.tile0, smem, gc, err);                                 \
+            mp_vh::DISPATCH<CIN, CM>(J, t - J.tile0, smem, gc, err);                                 \
             __syncthreads(); /* every thread has read next_item */                                  \
             if (threadIdx.x == 0) next_item = (int)gridDim.x + atomicAdd(counter, 1);              \
             __syncthreads();                                                                        \
             t = next_item;                                                                          \
         }                                                                                           \
     }                                                                                               \
-    __global__ void __launch_bounds__(MP_VH_NT, 3)                                                  \
+    __global__ void __launch_bounds__(MP_VH_NT, MINB)                                                  \
         NAME##_single(const __grid_constant__ MPJob job, int *err)                                  \
     {                                                                                               \
         extern __shared__ float4 mp_vh_dsmem4[];                                                    \
@@ -423,5 +463,10 @@ __device__ __forceinline__ void vh_init(float *smem)
         mp_vh::vh_init(smem);                                                                       \
         uint32_t gc = 0;                                                                            \
         for (int t = blockIdx.x; t < job.ntiles; t += gridDim.x)                                    \
-            mp_vh::vh_dispatch<CIN, CM>(job, t, smem, gc, err);                                         \
+            mp_vh::DISPATCH<CIN, CM>(job, t, smem, gc, err);                                         \
     }
+
+// Radii 1..MP_VH_RMAX (3 CTAs per SM) and the buckets above (2 CTAs per SM:
+// the larger window needs more registers).
+#define MP_VH_KERNELS(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch, 3)
+#define MP_VH_KERNELS_BIG(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_big, 2)

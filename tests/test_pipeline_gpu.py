@@ -170,16 +170,26 @@ def test_pointwise_before_gaussian_keeps_zero_padding(gpu, rng):
 
 
 def test_channel_preserving_gaussian_strips_and_mirror(gpu, rng):
-    # RGB / RGBA blur across several strips, a per-channel prologue and
-    # epilogue, a mirrored output, radii inside (2, 4, 12) and beyond (14)
-    # the compiled range
-    for c in (3, 4):
-        for sigma in (0.4, 1.3, 4.0, 4.4):
+    # 1-channel / RGB / RGBA blur across several strips, a per-channel
+    # prologue and epilogue, a mirrored output; radii 2, 4 and 12 (compiled
+    # one by one), 14, 20 and 24 (the buckets 16, 20, 24)
+    for c in (1, 3, 4):
+        for sigma in (0.4, 1.3, 4.0, 4.4, 6.5, 8.0):
             spec = [dict(op="colorize", lo=(1.2, 0.7, 0.9)), dict(op="gaussian", lo=(sigma,)),
                     dict(op="adjust_gamma", lo=(0.8, 1.0)), dict(op="fliplr")]
-            xs = [rng.random((70, 301, c), dtype=np.float32), rng.random((9, 5, c), dtype=np.float32)]
+            shape = (70, 301) if c == 1 else (70, 301, c)
+            small = (9, 5) if c == 1 else (9, 5, c)
+            xs = [rng.random(shape, dtype=np.float32), rng.random(small, dtype=np.float32)]
             check_spec(spec, xs)
             check_spec(spec[1:2], xs[:1])
+
+
+def test_gaussian_launch_mixing_radius_buckets(gpu, rng):
+    # one batch whose radii fall on both sides of 12: two launches of the
+    # streaming kernels, images in radius order
+    spec = [dict(op="gaussian", random=True, lo=(0.5,), hi=(7.5,))]
+    xs = [rng.random((40 + 3 * i, 90 - 2 * i, 3), dtype=np.float32) for i in range(12)]
+    check_spec(spec, xs, seed=5)
 
 
 def test_chunking_over_l2_budget(gpu, rng):
