@@ -122,21 +122,28 @@ __device__ void mp_point_adj_tile(const MPJob &J, int t, float *red)
 #pragma unroll
     for (int k = 0; k < MP_MAX_PW; ++k) pacc[k][0] = pacc[k][1] = pacc[k][2] = 0.f;
     if (x < J.w) {
-#pragma unroll 1
+        // the tile's 4 rows are loaded before any is processed (their loads
+        // overlap instead of waiting on each row's compute)
+        float x0[4][4], g0[4][4];
+#pragma unroll
         for (int i = 0; i < 4; ++i) {
-            const int y = ty * 4 + i;
-            if (y >= J.h) break;
-            float x0[4], g[4];
+            const int y = min(ty * 4 + i, J.h - 1);
             const float *p = J.src + (size_t)y * J.src_pitch + (size_t)x * cin;
             const float *gp = J.aux + (size_t)y * J.aux_pitch + (size_t)x * cout;
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                x0[c] = (c < cin) ? __ldg(p + c) : 0.f;
-                g[c] = (c < cout) ? __ldg(gp + c) : 0.f;
+                x0[i][c] = (c < cin) ? __ldg(p + c) : 0.f;
+                g0[i][c] = (c < cout) ? __ldg(gp + c) : 0.f;
             }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int y = ty * 4 + i;
+            if (y >= J.h) break;
+            float g[4] = {g0[i][0], g0[i][1], g0[i][2], g0[i][3]};
 #pragma unroll 1
             for (int k = n - 1; k >= 0; --k) {
-                float v[4] = {x0[0], x0[1], x0[2], x0[3]};
+                float v[4] = {x0[i][0], x0[i][1], x0[i][2], x0[i][3]};
                 int c = cin;
 #pragma unroll 1
                 for (int j = 0; j < k; ++j) {

@@ -449,12 +449,16 @@ size_t mp_ro_smem(int buf_floats);
 // kernel code names the family: the source channel count (1, 3, 4) for the
 // single-channel family (cmid 1), 4 + C (7, 8) for the channel-preserving
 // family on C = 3 or 4 interleaved channels, plus 16 for the radius buckets
-// above MP_VH_RMAX (1-channel sources, RGB and RGBA only); -1 if no kernel
+// above MP_VH_RMAX (1-channel sources, RGB and RGBA only), plus 32 for the
+// dot mode of the gaussian's adjoint (mp_vd*.cu); -1 if no kernel
 // takes (cin, cmid, radius).  mp_vh_bucket is the radius a job runs with
 // (its strip halo).  Strips are counted in columns: pixels when cm = 1,
 // floats of the interleaved row otherwise.
 int mp_vh_code(int cin, int cmid, int radius);
 int mp_vh_bucket(int radius);
+// Code of the d sigma dot mode (code + 32) for c-channel images, radii up
+// to MP_VH_RMAX; -1 if none.
+int mp_vh_dot_code(int c, int radius);
 int mp_vh_strip(int radius, int cm);
 int mp_vh_fit_strip(int radius, int w, int cm);
 MPStatus mp_vh_prepare(int code, int *ctas_per_sm);

@@ -756,6 +756,39 @@ static MPStatus mp_vh_run_single(const Seg &sg, const MPImage &in, const MPImage
     return mp_vh_launch_single(code, J, grid, err, s);
 }
 
+// Adds one launch of a rotate stage over images (sgs[i]: srcs[i] -> dsts[i])
+// on the footprint-staged kernel when every image can take it; *added says
+// whether it did (otherwise the caller builds the tile kernel's launch).
+static MPStatus mp_add_rot(MPTables &T, std::vector<MPLaunch> &launches, const std::vector<Seg> &sgs,
+                           const std::vector<MPImage> &srcs, const std::vector<MPImage> &dsts, bool *added)
+{
+    *added = false;
+    if (sgs.empty()) return MILLIPYDE_SUCCESS;
+    for (size_t i = 0; i < sgs.size(); ++i)
+        if (!mp_rot_ok(sgs[i], srcs[i])) return MILLIPYDE_SUCCESS;
+    std::vector<MPJob> js(sgs.size());
+    double bytes = 0.0;
+    int bufmax = 0;
+    for (size_t i = 0; i < sgs.size(); ++i) {
+        if (mp_fill_job_rot(js[i], sgs[i], srcs[i], dsts[i]) != MILLIPYDE_SUCCESS) return MILLIPYDE_SUCCESS;
+        bufmax = std::max(bufmax, mp_rot_buf_floats(js[i]));
+        bytes += 4.0 * ((double)srcs[i].height * srcs[i].width * srcs[i].channels +
+                        (double)dsts[i].height * dsts[i].width * dsts[i].channels);
+    }
+    int grid = 0;
+    const int c0 = sgs[0].cin;
+    if (!mp_rot_setup(c0, bufmax, &grid)) return MILLIPYDE_SUCCESS;
+    const size_t nl = launches.size();
+    MPStatus st = T.add(launches, MPK_RSTREAM, c0, mp_ro_smem(bufmax), js, bytes);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    if (launches.size() > nl) {
+        launches.back().grid = grid;
+        launches.back().gauss[0] = bufmax;
+    }
+    *added = true;
+    return MILLIPYDE_SUCCESS;
+}
+
 // Adds one launch of a gaussian stage over images (sgs[i]: srcs[i] ->
 // dsts[i]) with the fastest kernel that takes every image: the mp_vh.cuh
 // streaming kernels, the strip-streaming kernel, else the tile kernel.  The
@@ -996,42 +1029,18 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             int tw = 0, th = 0;
             size_t smem = 0;
             if (kind == MPK_ROTATE) {
-                // footprint-staged kernel when every image of the launch can take it
-                bool ok = true;
-                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
-                    const MPImage &src = (k == 0) ? in[ch.imgs[q]] : inter[q][k - 1];
-                    ok = mp_rot_ok(segs[ch.imgs[q]][k], src);
-                }
-                std::vector<MPJob> js;
-                double bytes = 0.0;
-                int bufmax = 0;
-                for (size_t q = 0; q < ch.imgs.size() && ok; ++q) {
+                std::vector<Seg> sgs;
+                std::vector<MPImage> srcs, dsts;
+                for (size_t q = 0; q < ch.imgs.size(); ++q) {
                     const int img = ch.imgs[q];
-                    const Seg &sg = segs[img][k];
-                    const MPImage &src = (k == 0) ? in[img] : inter[q][k - 1];
-                    const MPImage &dst = (k + 1 == nseg) ? out[img] : inter[q][k];
-                    MPJob J;
-                    if (mp_fill_job_rot(J, sg, src, dst) != MILLIPYDE_SUCCESS) {
-                        ok = false;
-                        break;
-                    }
-                    bufmax = std::max(bufmax, mp_rot_buf_floats(J));
-                    bytes += 4.0 * ((double)src.height * src.width * src.channels +
-                                    (double)dst.height * dst.width * dst.channels);
-                    js.push_back(J);
+                    sgs.push_back(segs[img][k]);
+                    srcs.push_back((k == 0) ? in[img] : inter[q][k - 1]);
+                    dsts.push_back((k + 1 == nseg) ? out[img] : inter[q][k]);
                 }
-                int grid = 0;
-                const int c0 = segs[ch.imgs[0]][k].cin;
-                if (ok && mp_rot_setup(c0, bufmax, &grid)) {
-                    const size_t nl = P->launches.size();
-                    st = T.add(P->launches, MPK_RSTREAM, c0, mp_ro_smem(bufmax), js, bytes);
-                    if (st != MILLIPYDE_SUCCESS) return st;
-                    if (P->launches.size() > nl) {
-                        P->launches.back().grid = grid;
-                        P->launches.back().gauss[0] = bufmax;
-                    }
-                    continue;
-                }
+                bool added = false;
+                st = mp_add_rot(T, P->launches, sgs, srcs, dsts, &added);
+                if (st != MILLIPYDE_SUCCESS) return st;
+                if (added) continue;
             }
             if (kind == MPK_GAUSS) {
                 std::vector<Seg> sgs;
@@ -1932,6 +1941,18 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
                 st = mp_add_gauss(T, P.launches, sgs, srcs, dsts);
                 continue;
             } else {
+                if (kind == MPK_ROTATE) {
+                    std::vector<Seg> sgs;
+                    std::vector<MPImage> srcs, dsts;
+                    for (int q = 0; q < nb; ++q) {
+                        sgs.push_back(seg_of(q, k));
+                        srcs.push_back(a_img(q, k));
+                        dsts.push_back(a_img(q, k + 1));
+                    }
+                    bool added = false;
+                    st = mp_add_rot(T, P.launches, sgs, srcs, dsts, &added);
+                    if (st != MILLIPYDE_SUCCESS || added) continue;
+                }
                 for (int q = 0; q < nb && st == MILLIPYDE_SUCCESS; ++q) {
                     MPJob J;
                     st = mp_fill_job(J, seg_of(q, k), a_img(q, k), a_img(q, k + 1), 0, 0);
@@ -1994,8 +2015,63 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
                 }
                 size_t smem = 0;
                 // d sigma = <g, (W' (x) W + W (x) W') a_k>: two dot-mode launches,
-                // only when sigma wants a gradient
-                for (int pass = 0; pass < 2 && wants(k) && st == MILLIPYDE_SUCCESS; ++pass) {
+                // only when sigma wants a gradient; the streaming kernels' dot
+                // mode when every image can take it (images in radius order),
+                // else the tile kernel's
+                bool vdot = wants(k) && st == MILLIPYDE_SUCCESS;
+                int dcode = -1, dgrid = 0;
+                std::vector<int> qord(nb);
+                for (int q = 0; q < nb; ++q) qord[q] = q;
+                long long drows = 0;
+                for (int q = 0; q < nb && vdot; ++q) {
+                    const Seg sg = seg_of(q, k);
+                    const int r = (int)ceil(3.0 * sg.core_p[0]);
+                    const int c = mp_vh_dot_code(sg.cin, r);
+                    vdot = c >= 0 && (dcode < 0 || c == dcode) && mp_vh_ok(sg, a_img(q, k));
+                    dcode = c;
+                    const int cm = (c & 15) > 4 ? sg.cin : 1;
+                    const int sw = mp_vh_fit_strip(r, sh[k].w, cm);
+                    drows += (long long)((sh[k].w * cm + sw - 1) / sw) * sh[k].h;
+                }
+                int dcps = 0;
+                if (vdot && mp_vh_prepare(dcode, &dcps) != MILLIPYDE_SUCCESS) {
+                    cudaGetLastError();
+                    vdot = false;
+                }
+                if (vdot) {
+                    dgrid = dcps * mp_num_sms();
+                    std::stable_sort(qord.begin(), qord.end(), [&](int a, int b) {
+                        return seg_of(a, k).core_p[0] < seg_of(b, k).core_p[0];
+                    });
+                    const int rs = mp_vh_rows(drows, dgrid);
+                    for (int pass = 0; pass < 2 && st == MILLIPYDE_SUCCESS; ++pass) {
+                        std::vector<MPJob> jd(nb);
+                        for (int i = 0; i < nb && st == MILLIPYDE_SUCCESS; ++i) {
+                            const int q = qord[i];
+                            const Seg sg = seg_of(q, k);
+                            const MPImage go = gout_img(q);
+                            MPJob &J = jd[i];
+                            st = mp_fill_job_vh(J, sg, a_img(q, k), go, rs);
+                            if (st != MILLIPYDE_SUCCESS) break;
+                            float w[MP_MAX_TAPS], dw[MP_MAX_TAPS];
+                            mp_gauss_taps(sg.core_p[0], J.radius, w, dw);
+                            for (int t = 0; t < 2 * J.radius + 1; ++t) {
+                                J.wts[t] = pass == 0 ? dw[t] : w[t];
+                                J.wts_h[t] = pass == 0 ? w[t] : dw[t];
+                            }
+                            J.dot = 1;
+                            J.aux = (const float *)go.data;
+                            J.aux_pitch = go.pitch / 4;
+                            J.dst = nullptr;
+                            J.acc = dparams + ((size_t)(b0 + q) * nops + k) * 3;
+                        }
+                        if (st != MILLIPYDE_SUCCESS) break;
+                        const size_t nl = P.launches.size();
+                        st = T.add(P.launches, MPK_VH, dcode, 0, jd, 0.0);
+                        if (st == MILLIPYDE_SUCCESS && P.launches.size() > nl) P.launches.back().grid = dgrid;
+                    }
+                }
+                for (int pass = 0; pass < 2 && wants(k) && !vdot && st == MILLIPYDE_SUCCESS; ++pass) {
                     std::vector<std::pair<Seg, std::pair<MPImage, MPImage>>> it2;
                     for (int q = 0; q < nb; ++q) it2.push_back({seg_of(q, k), {a_img(q, k), gout_img(q)}});
                     std::vector<MPJob> jd;

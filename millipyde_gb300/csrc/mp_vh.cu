@@ -19,6 +19,9 @@ MP_VH_DECL(mp_vc_c4)
 MP_VH_DECL(mp_vb_c1)
 MP_VH_DECL(mp_vb_c3)
 MP_VH_DECL(mp_vb_c4)
+MP_VH_DECL(mp_vd_c1)
+MP_VH_DECL(mp_vd_c3)
+MP_VH_DECL(mp_vd_c4)
 
 int mp_vh_code(int cin, int cmid, int radius)
 {
@@ -29,6 +32,12 @@ int mp_vh_code(int cin, int cmid, int radius)
     if (radius <= MP_VH_RMAX) return code;
     // buckets: channel-keeping kernels only (1-channel source, RGB, RGBA)
     return (code == 1 || code == 7 || code == 8) ? code + 16 : -1;
+}
+
+int mp_vh_dot_code(int c, int radius)
+{
+    const int code = mp_vh_code(c, c, radius);
+    return (code == 1 || code == 7 || code == 8) ? code + 32 : -1;
 }
 
 int mp_vh_bucket(int radius) { return radius <= MP_VH_RMAX ? radius : (radius <= 16 ? 16 : (radius <= 20 ? 20 : 24)); }
@@ -47,6 +56,9 @@ static const void *mp_vh_fn(int code, bool single)
     case 17: return single ? (const void *)mp_vb_c1_single : (const void *)mp_vb_c1_batch;
     case 23: return single ? (const void *)mp_vb_c3_single : (const void *)mp_vb_c3_batch;
     case 24: return single ? (const void *)mp_vb_c4_single : (const void *)mp_vb_c4_batch;
+    case 33: return single ? (const void *)mp_vd_c1_single : (const void *)mp_vd_c1_batch;
+    case 39: return single ? (const void *)mp_vd_c3_single : (const void *)mp_vd_c3_batch;
+    case 40: return single ? (const void *)mp_vd_c4_single : (const void *)mp_vd_c4_batch;
     default: return nullptr;
     }
 }

@@ -106,10 +106,11 @@ __device__ __forceinline__ float2 prologue(const float *slot, bool in0, bool in1
 
 // Shared memory of one CTA (floats): 2 mbarriers + taps (64 floats), two
 // horizontal tiles [2][VR][VW], two staging buffers [2][NW][VR][64*PX]
-// (PX = floats staged per column: CIN when CM = 1, else 1).
+// (PX = floats staged per column: CIN when CM = 1, else 1), then the 64
+// horizontal taps of the dot mode.
 __host__ __device__ constexpr int mp_vh_smem_floats(int cin, int cm)
 {
-    return 64 + 64 + 2 * MP_VH_VR * MP_VH_VW + 2 * MP_VH_VR * 2 * MP_VH_NT * (cm == 1 ? cin : 1);
+    return 64 + 64 + 2 * MP_VH_VR * MP_VH_VW + 2 * MP_VH_VR * 2 * MP_VH_NT * (cm == 1 ? cin : 1) + 64;
 }
 
 // Channel of interleaved float column f (f may be negative: halo columns).
@@ -129,7 +130,11 @@ __device__ __forceinline__ int chan_of(int f)
 // window rows of each symmetric tap pair before multiplying (R + 1 tap
 // registers instead of 2R + 1) and the horizontal pass consumes the tile row
 // in order.
-template <int CIN, int CM, int R>
+// DOT: the d sigma mode of the gaussian's adjoint.  The horizontal pass
+// uses J.wts_h (the vertical pass J.wts), nothing is stored, and the sum of
+// output * J.aux (the output-space gradient) over the item is added to
+// J.acc[0] in FP64 (one atomic per warp and item).
+template <int CIN, int CM, int R, bool DOT = false>
 __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32_t &gcount, int *err)
 {
     constexpr bool BIG = R > MP_VH_RMAX;
@@ -149,6 +154,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     float *taps = smem + 64;
     float *tile = smem + 128;
     float *stg = tile + 2 * VR * VW;                      // [2][NW][VR][BOXW]
+    float *taps_h = stg + 2 * GF;                         // DOT: horizontal taps
 
     const int sy = lt / J.tiles_x, sx = lt - sy * J.tiles_x;
     const int H = J.h, W = J.w * CM;                      // W in columns
@@ -167,6 +173,9 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
         if (tid < 64) taps[tid] = (tid >= sh && tid < NTAP - sh) ? J.wts[tid - sh] : 0.f;
     } else {
         if (tid < 64) taps[tid] = tid < NTAP ? J.wts[tid] : 0.f;
+    }
+    if constexpr (DOT) {
+        if (tid < 64) taps_h[tid] = tid < NTAP ? J.wts_h[tid] : 0.f;
     }
     const PwFast pro = mp_pw_fast(J.pro);
     const bool grey_only = J.pro.n == 1 && pro.op == MP_OP_RGB2GREY;
@@ -254,6 +263,18 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     for (int m = 0; m < NW2; ++m) w2[m] = make_float2(taps[m], taps[m]);
     // tap m of 2R + 1 (symmetric storage for the buckets)
     auto tap = [&](int m) -> float { return BIG ? w2[m <= R ? m : 2 * R - m].x : w2[m].x; };
+    float hw[DOT ? NTAP : 1];
+    if constexpr (DOT) {
+#pragma unroll
+        for (int m = 0; m < NTAP; ++m) hw[m] = taps_h[m];
+    }
+    // horizontal tap m
+    auto htap = [&](int m) -> float {
+        if constexpr (DOT) return hw[m];
+        else return tap(m);
+    };
+    float dacc = 0.f;   // DOT: this thread's share of sum(out * aux)
+    const bool aux_vec = DOT && ((uintptr_t)J.aux & 15) == 0 && (J.aux_pitch & 3) == 0;
 
     float2 win[NWIN];
     bool alive = true;
@@ -317,8 +338,8 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                         float a0 = 0.f, a1 = 0.f;
 #pragma unroll
                         for (int m = 0; m < NTAP; ++m) {
-                            if (m & 1) a1 = fmaf(w2[m].x, x[E + k + m], a1);
-                            else a0 = fmaf(w2[m].x, x[E + k + m], a0);
+                            if (m & 1) a1 = fmaf(htap(m), x[E + k + m], a1);
+                            else a0 = fmaf(htap(m), x[E + k + m], a0);
                         }
                         o[k] = a0 + a1;
                     }
@@ -336,10 +357,29 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
 #pragma unroll
                             for (int k = 0; k < 8; ++k) {
                                 const int t = 4 * q + u - E - k;   // = m * CM for tap m
-                                if (t >= 0 && t % CM == 0 && t / CM < NTAP) o[k] = fmaf(tap(t / CM), e4[u], o[k]);
+                                if (t >= 0 && t % CM == 0 && t / CM < NTAP) o[k] = fmaf(htap(t / CM), e4[u], o[k]);
                             }
                         }
                     }
+                }
+                if constexpr (DOT) {
+                    const float *arow = J.aux + (size_t)y * J.aux_pitch;
+                    if (aux_vec && xo0 + 8 <= W) {
+                        const float4 p = ld4(arow + xo0), q = ld4(arow + xo0 + 4);
+                        dacc = fmaf(o[0], p.x, dacc);
+                        dacc = fmaf(o[1], p.y, dacc);
+                        dacc = fmaf(o[2], p.z, dacc);
+                        dacc = fmaf(o[3], p.w, dacc);
+                        dacc = fmaf(o[4], q.x, dacc);
+                        dacc = fmaf(o[5], q.y, dacc);
+                        dacc = fmaf(o[6], q.z, dacc);
+                        dacc = fmaf(o[7], q.w, dacc);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            if (xo0 + k < W) dacc = fmaf(o[k], arow[xo0 + k], dacc);
+                    }
+                    continue;
                 }
                 if (epi.n) {
                     if constexpr (CM == 1) {
@@ -391,6 +431,11 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
         }
     }
     gcount = g0 + (uint32_t)ngroups;
+    if constexpr (DOT) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dacc += __shfl_down_sync(0xffffffffu, dacc, o);
+        if (lane == 0 && alive) atomicAdd(J.acc, (double)dacc);
+    }
 }
 
 template <int CIN, int CM>
@@ -403,6 +448,20 @@ __device__ __forceinline__ void vh_dispatch(const MPJob &J, int lt, float *smem,
         MP_VH_CASE(7) MP_VH_CASE(8) MP_VH_CASE(9) MP_VH_CASE(10) MP_VH_CASE(11) MP_VH_CASE(12)
 #undef MP_VH_CASE
     default: break;   // the planner never sends other radii here
+    }
+}
+
+// The d sigma dot mode, radii 1..MP_VH_RMAX.
+template <int CIN, int CM>
+__device__ __forceinline__ void vh_dispatch_dot(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
+{
+    switch (J.radius) {
+#define MP_VH_CASE(RR) \
+    case RR: vh_item<CIN, CM, RR, true>(J, lt, smem, gc, err); break;
+        MP_VH_CASE(1) MP_VH_CASE(2) MP_VH_CASE(3) MP_VH_CASE(4) MP_VH_CASE(5) MP_VH_CASE(6)
+        MP_VH_CASE(7) MP_VH_CASE(8) MP_VH_CASE(9) MP_VH_CASE(10) MP_VH_CASE(11) MP_VH_CASE(12)
+#undef MP_VH_CASE
+    default: break;
     }
 }
 
@@ -466,7 +525,13 @@ __device__ __forceinline__ void vh_init(float *smem)
             mp_vh::DISPATCH<CIN, CM>(job, t, smem, gc, err);                                         \
     }
 
-// Radii 1..MP_VH_RMAX (3 CTAs per SM) and the buckets above (2 CTAs per SM:
-// the larger window needs more registers).
+// Radii 1..MP_VH_RMAX and the d sigma dot mode (3 CTAs per SM; the dot
+// mode's second tap set costs a few spilled bytes at the largest radii), and
+// the buckets above MP_VH_RMAX (2 CTAs per SM: the larger window needs more
+// registers).
 #define MP_VH_KERNELS(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch, 3)
 #define MP_VH_KERNELS_BIG(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_big, 2)
+#ifndef MP_VH_DOT_MINB
+#define MP_VH_DOT_MINB 3
+#endif
+#define MP_VH_KERNELS_DOT(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_dot, MP_VH_DOT_MINB)

@@ -131,6 +131,30 @@ def test_config5_chain_vs_torch_reference(gpu):
     assert rel(delta.grad, dl2.grad) < 2e-3
 
 
+@pytest.mark.parametrize("C", [1, 3, 4])
+def test_sigma_gradient_every_channel_count(gpu, C):
+    """d sigma and dx of a lone gaussian on 1-, 3- and 4-channel batches:
+    radii 3, 6, 11, 12 (the streaming kernels' dot mode), then a batch with
+    radius 14 in it (the tile kernel's dot mode for the whole launch)."""
+    torch.manual_seed(3 + C)
+    B, H, W = 4, 40, 52
+    for sigmas in ((0.7, 1.9, 3.6, 3.9), (4.6, 1.0, 2.0, 3.0)):
+        x = torch.rand(B, H, W, C, device="cuda")
+        sigma = torch.tensor(sigmas, dtype=torch.float64, device="cuda").requires_grad_()
+        Wt = torch.randn(B, H, W, C, device="cuda")
+        xg = x.clone().requires_grad_()
+        y = mp_pipeline(xg, [("gaussian", sigma)])
+        y = y.reshape(B, H, W, C)
+        (y * Wt).sum().backward()
+        x64 = x.double().clone().requires_grad_()
+        sg2 = sigma.detach().clone().requires_grad_()
+        y64 = ref_gaussian(x64, sg2)
+        (y64 * Wt.double()).sum().backward()
+        assert float((y.double() - y64).abs().max()) <= TOL
+        assert rel(xg.grad, x64.grad) < 2e-4
+        assert rel(sigma.grad, sg2.grad) < 2e-3
+
+
 def test_pointwise_params_and_permutations(gpu):
     torch.manual_seed(2)
     B, H, W = 3, 40, 56
