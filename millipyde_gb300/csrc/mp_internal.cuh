@@ -27,9 +27,11 @@
 // segments without a prologue whose source rows are TMA-legal.
 // VH is the streaming gaussian of mp_vh.cuh (single-channel and
 // channel-preserving families), for radii up to MP_VH_RMAX.
+// RADJ / RDTH are the rotate adjoint's dx = R^T g and d theta passes on the
+// footprint-staged kernel (variant = 8 * mode + channels).
 enum MPKind {
     MPK_POINT = 0, MPK_GAUSS = 1, MPK_ROTATE = 2, MPK_TRANSPOSE = 3, MPK_GSTREAM = 4, MPK_RSTREAM = 5,
-    MPK_VH = 8
+    MPK_RADJ = 6, MPK_RDTH = 7, MPK_VH = 8
 };
 #define MP_VH_RMAX 12
 #define MP_VH_RBIG 24   // largest bucket radius of the mp_vh.cuh kernels

@@ -466,7 +466,9 @@ static bool mp_rot_ok(const Seg &sg, const MPImage &in)
     return mp_get_encode_tiled() != nullptr;
 }
 
-static MPStatus mp_fill_job_rot(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out)
+static MPStatus mp_fill_job_rot(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out, bool adj = false);
+
+static MPStatus mp_fill_job_rot(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out, bool adj)
 {
     MPStatus st = mp_fill_job(J, sg, in, out, 0, 0);   // source/destination, cos/sin, epilogue
     if (st != MILLIPYDE_SUCCESS) return st;
@@ -478,9 +480,11 @@ static MPStatus mp_fill_job_rot(MPJob &J, const Seg &sg, const MPImage &in, cons
     const double c = fabs((double)J.cosq) / (double)(1LL << (MP_FIX_FRAC - 1));
     const double sn = fabs((double)J.sinq) / (double)(1LL << (MP_FIX_FRAC - 1));
     // (+3: floor spread, bilinear neighbour, rounding; +1: the margin pixel
-    // before the footprint)
-    const int bw = (int)ceil((TW - 1) * c + (TH - 1) * sn + 1e-6) + 4;
-    const int bh = (int)ceil((TW - 1) * sn + (TH - 1) * c + 1e-6) + 4;
+    // before the footprint).  The adjoint's box of g around a source tile
+    // needs +7: two margin pixels before, the floor spread, three candidates
+    // after the first, one pixel of float rounding.
+    const int bw = (int)ceil((TW - 1) * c + (TH - 1) * sn + 1e-6) + (adj ? 7 : 4);
+    const int bh = (int)ceil((TW - 1) * sn + (TH - 1) * c + 1e-6) + (adj ? 7 : 4);
     J.bxw = (bw * C + 3 + 3) & ~3;
     J.byh = bh;
     if (J.bxw > 256 || J.byh > 256) return MP_ERROR_TOO_LARGE;
@@ -652,7 +656,8 @@ struct MPTables {
             L.njobs++;
         }
         if (L.njobs == 0) return MILLIPYDE_SUCCESS;
-        if (kind < MPK_POINT_ADJ && kind != MPK_GSTREAM && kind != MPK_RSTREAM && kind != MPK_VH) {
+        if (kind < MPK_POINT_ADJ && kind != MPK_GSTREAM && kind != MPK_RSTREAM && kind != MPK_VH &&
+            kind != MPK_RADJ && kind != MPK_RDTH) {
             MPStatus e = mp_prepare_kind(kind, variant, smem);
             if (e != MILLIPYDE_SUCCESS) return e;
         }
@@ -1090,7 +1095,7 @@ static MPStatus mp_plan_launch_one(const MPPlanImpl *P, size_t idx, cudaStream_t
         return mp_vh_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles, L.grid,
                             P->err, P->counters + idx, s);
     }
-    if (L.kind == MPK_RSTREAM)
+    if (L.kind == MPK_RSTREAM || L.kind == MPK_RADJ || L.kind == MPK_RDTH)
         return mp_ro_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles,
                             L.gauss[0], L.grid, P->err, s);
     if (L.kind == MPK_GSTREAM)
@@ -1826,6 +1831,59 @@ static void mp_gauss_taps(double sigma, int r, float *w, float *dw)
     }
 }
 
+// Rotate adjoint of op k on the footprint-staged kernel: one RADJ launch
+// (dx = R^T g, boxes of g around each source tile) and, when theta wants a
+// gradient, one RDTH launch (d theta over output tiles, boxes of the
+// source).  Returns false, adding nothing, when some image's rows are not
+// TMA-legal or a box does not fit (the caller runs the gather kernel);
+// errors of the launches it added go to *st.
+template <class SegOf, class AImg, class GoImg, class GiImg, class Acc>
+static bool mp_rot_adj_fp(MPTables &T, std::vector<MPLaunch> &launches, int nb, SegOf seg_of, AImg a_img,
+                          GoImg gout_img, GiImg gin_img, bool want_theta, Acc acc_of, MPStatus *st)
+{
+    std::vector<MPJob> ja(nb), jt(want_theta ? nb : 0);
+    int bufa = 0, buft = 0;
+    for (int q = 0; q < nb; ++q) {
+        const Seg sg = seg_of(q);
+        const MPImage go = gout_img(q), gi = gin_img(q), a = a_img(q);
+        if (!mp_rot_ok(sg, go) || (want_theta && !mp_rot_ok(sg, a))) return false;
+        if (mp_fill_job_rot(ja[q], sg, go, gi, true) != MILLIPYDE_SUCCESS) return false;
+        const double th_r = sg.core_p[0] * MP_DEG2RAD;
+        ja[q].cth = (float)cos(th_r);
+        ja[q].sth = (float)sin(th_r);
+        bufa = std::max(bufa, mp_rot_buf_floats(ja[q]));
+        if (want_theta) {
+            if (mp_fill_job_rot(jt[q], sg, a, go) != MILLIPYDE_SUCCESS) return false;
+            jt[q].cth = ja[q].cth;
+            jt[q].sth = ja[q].sth;
+            jt[q].aux = (const float *)go.data;
+            jt[q].aux_pitch = go.pitch / 4;
+            jt[q].dst = nullptr;
+            jt[q].acc = acc_of(q);
+            buft = std::max(buft, mp_rot_buf_floats(jt[q]));
+        }
+    }
+    const int C = seg_of(0).cin;
+    int ga = 0, gt = 0;
+    if (!mp_rot_setup(8 * 1 + C, bufa, &ga)) return false;
+    if (want_theta && !mp_rot_setup(8 * 2 + C, buft, &gt)) return false;
+    size_t nl = launches.size();
+    *st = T.add(launches, MPK_RADJ, 8 * 1 + C, mp_ro_smem(bufa), ja, 0.0);
+    if (*st == MILLIPYDE_SUCCESS && launches.size() > nl) {
+        launches.back().grid = ga;
+        launches.back().gauss[0] = bufa;
+    }
+    if (*st == MILLIPYDE_SUCCESS && want_theta) {
+        nl = launches.size();
+        *st = T.add(launches, MPK_RDTH, 8 * 2 + C, mp_ro_smem(buft), jt, 0.0);
+        if (*st == MILLIPYDE_SUCCESS && launches.size() > nl) {
+            launches.back().grid = gt;
+            launches.back().gauss[0] = buft;
+        }
+    }
+    return true;
+}
+
 #define MP_BWD_SCRATCH_BYTES (2048ull << 20)
 
 extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const double *params, const float *x,
@@ -2094,6 +2152,12 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
                     }
                     if (st == MILLIPYDE_SUCCESS) st = add_launch(MPK_GAUSS, smem, jd);
                 }
+            } else if (ops[k] == MP_OP_ROTATE &&
+                       mp_rot_adj_fp(
+                           T, P.launches, nb, [&](int q) { return seg_of(q, k); },
+                           [&](int q) { return a_img(q, k); }, gout_img, gin_img, wants(k),
+                           [&](int q) { return dparams + ((size_t)(b0 + q) * nops + k) * 3; }, &st)) {
+                // dx = R^T g and d theta on the footprint-staged kernel
             } else if (ops[k] == MP_OP_ROTATE) {
                 for (int q = 0; q < nb && st == MILLIPYDE_SUCCESS; ++q) {
                     MPJob J;

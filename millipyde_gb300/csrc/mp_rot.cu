@@ -45,17 +45,44 @@ __device__ __forceinline__ void ro_origin(const MPJob &J, int lt, int TW, int TH
     *by = (int)(sy_min >> MP_FIX_FRAC) - 1;
 }
 
+// Kernel modes: the forward rotate; the adjoint's dx = R^T g (tiles of the
+// source image, boxes of g); the adjoint's d theta (output tiles, boxes of
+// the source, as the forward).
+enum { RO_FWD = 0, RO_ADJ = 1, RO_DTH = 2 };
+
+// Box origin (pixels) of source tile lt in the adjoint: the output pixels
+// whose samples can use the tile's pixels lie around R(-theta)(q - c) + c;
+// two pixels of margin before the exact minimum (the candidate window starts
+// one pixel before the float position, which may round below the exact one).
+__device__ __forceinline__ void ro_origin_adj(const MPJob &J, int lt, int TW, int TH, int *bx, int *by, int *x0,
+                                              int *y0)
+{
+    const int ty = lt / J.tiles_x, tx = lt - ty * J.tiles_x;
+    *x0 = tx * TW;
+    *y0 = ty * TH;
+    const long long W = J.w, H = J.h;
+    const long long xa = 2LL * *x0 - W, xb = 2LL * (*x0 + TW - 1) - W;
+    const long long ya = 2LL * *y0 - H, yb = 2LL * (*y0 + TH - 1) - H;
+    const long long cq = J.cosq, sq = J.sinq;
+    // min over the four corners of px = cq*X2 + sq*Y2 and py = -sq*X2 + cq*Y2
+    const long long px_min = min(cq * xa, cq * xb) + min(sq * ya, sq * yb) + (W << (MP_FIX_FRAC - 1));
+    const long long py_min = min(-sq * xa, -sq * xb) + min(cq * ya, cq * yb) + (H << (MP_FIX_FRAC - 1));
+    *bx = (int)(px_min >> MP_FIX_FRAC) - 2;
+    *by = (int)(py_min >> MP_FIX_FRAC) - 2;
+}
+
 // Per-buffer tile record written by the issuing thread: footprint origin
 // (pixels) and output tile origin.
 struct RoTile {
     int bx, by, x0, y0;
 };
 
-template <int C>
+template <int C, int MODE = RO_FWD>
 __device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uint64_t *bar, RoTile *rec)
 {
     int bx, by, x0, y0;
-    ro_origin(J, lt, mp_ro_tw(C), mp_ro_th(C), &bx, &by, &x0, &y0);
+    if (MODE == RO_ADJ) ro_origin_adj(J, lt, mp_ro_tw(C), mp_ro_th(C), &bx, &by, &x0, &y0);
+    else ro_origin(J, lt, mp_ro_tw(C), mp_ro_th(C), &bx, &by, &x0, &y0);
     rec->bx = bx;
     rec->by = by;
     rec->x0 = x0;
@@ -152,6 +179,146 @@ __device__ __forceinline__ void ro_tile(const MPJob &J, const RoTile &T, const f
     else ro_tile_k<C, RO_EPI_LIST>(J, T, buf);
 }
 
+// Exact forward sample position of output pixel (x, y) in MP_FIX_FRAC
+// fixed point (the tile kernel's and the adjoint's arithmetic).
+__device__ __forceinline__ void ro_src_fixed(const MPJob &J, int x, int y, long long &sx, long long &sy)
+{
+    const long long W = J.w, H = J.h;
+    const long long X2 = 2LL * x - W, Y2 = 2LL * y - H;
+    sx = J.cosq * X2 - J.sinq * Y2 + (W << (MP_FIX_FRAC - 1));
+    sy = J.sinq * X2 + J.cosq * Y2 + (H << (MP_FIX_FRAC - 1));
+}
+
+__device__ __forceinline__ float ro_frac24(long long s)
+{
+    return (float)((int)((s >> (MP_FIX_FRAC - 24)) & 0xFFFFFF)) * 5.9604644775390625e-8f;
+}
+
+// Adjoint dx(q) = sum over output pixels p of w(p, q) g(p) for the pixels q
+// of one source tile: each q visits the 4 x 4 output pixels around
+// R(-theta)(q - c) + c, keeps those whose forward sample used q and applies
+// the forward's bilinear weight (positions exact in fixed point, stepped by
+// 2 cos / 2 sin: the map is affine).  g comes from the staged box; a
+// candidate outside it (not expected) is read from global memory.  The job's
+// source is g, its destination dx.
+template <int C>
+__device__ __forceinline__ void ro_adj_tile(const MPJob &J, const RoTile &T, const float *buf)
+{
+    constexpr int TW = mp_ro_tw(C), TH = mp_ro_th(C), NT = MP_RO_NT;
+    constexpr int RSTEP = NT / TW, NPX = TW * TH / NT;
+    const int bx = T.bx, by = T.by;
+    const int delta = bx * C - ((bx * C) & ~3);
+    const int bxw = J.bxw, bpx = (bxw - delta) / C, bh = J.byh;
+    const int qx = T.x0 + (threadIdx.x & (TW - 1));
+    const int qy0 = T.y0 + threadIdx.x / TW;
+    const int W = J.w, H = J.h;
+    if (qx >= W) return;
+    const float hw = 0.5f * (float)W, hh = 0.5f * (float)H;
+    const float ct = J.cth, st = J.sth;
+    const long long c2 = 2 * J.cosq, s2 = 2 * J.sinq;
+    const float *g = J.src;
+    const int gp = J.src_pitch, dp = J.dst_pitch;
+#pragma unroll 1
+    for (int i = 0; i < NPX; ++i) {
+        const int qy = qy0 + RSTEP * i;
+        if (qy >= H) break;
+        const float dxq = (float)qx - hw, dyq = (float)qy - hh;
+        const int px0 = (int)floorf(ct * dxq + st * dyq + hw) - 1;
+        const int py0 = (int)floorf(-st * dxq + ct * dyq + hh) - 1;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        long long sxr, syr;
+        ro_src_fixed(J, px0, py0, sxr, syr);
+#pragma unroll
+        for (int jy = 0; jy < 4; ++jy) {
+            const int py = py0 + jy;
+            const bool yok = py >= 0 && py < H;
+            long long sx = sxr, sy = syr;
+#pragma unroll
+            for (int jx = 0; jx < 4; ++jx) {
+                const int px = px0 + jx;
+                const int ex = qx - (int)(sx >> MP_FIX_FRAC), ey = qy - (int)(sy >> MP_FIX_FRAC);
+                if (yok && px >= 0 && px < W && (unsigned)ex <= 1u && (unsigned)ey <= 1u) {
+                    const float fx = ro_frac24(sx), fy = ro_frac24(sy);
+                    const float w = (ey ? fy : 1.0f - fy) * (ex ? fx : 1.0f - fx);
+                    const int ox = px - bx, oy = py - by;
+                    if ((unsigned)ox < (unsigned)bpx && (unsigned)oy < (unsigned)bh) {
+                        const float *v = buf + oy * bxw + ox * C + delta;
+#pragma unroll
+                        for (int c = 0; c < C; ++c) acc[c] = fmaf(w, v[c], acc[c]);
+                    } else {
+                        const float *v = g + (size_t)py * gp + (size_t)px * C;
+#pragma unroll
+                        for (int c = 0; c < C; ++c) acc[c] = fmaf(w, __ldg(v + c), acc[c]);
+                    }
+                }
+                sx += c2;
+                sy += s2;
+            }
+            sxr -= s2;
+            syr += c2;
+        }
+        float *d = J.dst + (size_t)qy * dp + (size_t)qx * C;
+#pragma unroll
+        for (int c = 0; c < C; ++c) d[c] = acc[c];
+    }
+}
+
+// Adjoint d theta over one output tile: sum over its pixels p of
+// g(p) . (d bilinear(x, s) / d s) . (d s / d theta), s = R(theta)(p - c) + c,
+// with x's neighbours from the staged box exactly as the forward reads them
+// and g (J.aux, output layout) from global memory.  Returns this thread's
+// share.
+template <int C>
+__device__ __forceinline__ float ro_dth_tile(const MPJob &J, const RoTile &T, const float *buf)
+{
+    constexpr int TW = mp_ro_tw(C), TH = mp_ro_th(C), NT = MP_RO_NT;
+    constexpr int RSTEP = NT / TW, NPX = TW * TH / NT;
+    const int bx = T.bx, by = T.by, x0 = T.x0, y0 = T.y0;
+    const int delta = bx * C - ((bx * C) & ~3);
+    const int bxw = J.bxw;
+    const int x = x0 + (threadIdx.x & (TW - 1));
+    const int yf = y0 + threadIdx.x / TW;
+    const int wo = J.wo, ho = J.ho;
+    if (x >= wo) return 0.f;
+    const long long W = J.w, H = J.h, cq = J.cosq, sq = J.sinq;
+    const long long X2 = 2LL * x - W, Y2 = 2LL * yf - H;
+    const long long rx0 = cq * X2 - sq * Y2 + (W << (MP_FIX_FRAC - 1)) - ((long long)bx << MP_FIX_FRAC);
+    const long long ry0 = sq * X2 + cq * Y2 + (H << (MP_FIX_FRAC - 1)) - ((long long)by << MP_FIX_FRAC);
+    int lx = (int)(rx0 >> (MP_FIX_FRAC - 24)), ly = (int)(ry0 >> (MP_FIX_FRAC - 24));
+    const int stx = (int)((-2LL * RSTEP * sq) >> (MP_FIX_FRAC - 24));
+    const int sty = (int)((2LL * RSTEP * cq) >> (MP_FIX_FRAC - 24));
+    const float hw = 0.5f * (float)W, hh = 0.5f * (float)H;
+    const float ct = J.cth, st = J.sth;
+    const float dxq = (float)x - hw;
+    const float *gcol = J.aux + (size_t)x * C;
+    float dth = 0.f;
+#pragma unroll 4
+    for (int i = 0; i < NPX; ++i) {
+        const int y = yf + RSTEP * i;
+        if (y < ho) {
+            const float fx = fmaf(__int_as_float(0x4B000000 | ((lx >> 1) & 0x7FFFFF)), 1.1920928955078125e-7f, -1.0f);
+            const float fy = fmaf(__int_as_float(0x4B000000 | ((ly >> 1) & 0x7FFFFF)), 1.1920928955078125e-7f, -1.0f);
+            const float *p0 = buf + (ly >> 24) * bxw + (lx >> 24) * C + delta;
+            const float *p1 = p0 + bxw;
+            const float gx = 1.0f - fx, gy = 1.0f - fy;
+            const float dyq = (float)y - hh;
+            const float dsx = (-st * dxq - ct * dyq) * 0.01745329252f;
+            const float dsy = (ct * dxq - st * dyq) * 0.01745329252f;
+            const float *gp = gcol + (size_t)y * J.aux_pitch;
+#pragma unroll
+            for (int k = 0; k < C; ++k) {
+                const float a = p0[k], b = p0[C + k], c = p1[k], d = p1[C + k];
+                const float dvx = gy * (b - a) + fy * (d - c);
+                const float dvy = gx * (c - a) + fx * (d - b);
+                dth = fmaf(__ldg(gp + k), dvx * dsx + dvy * dsy, dth);
+            }
+        }
+        lx += stx;
+        ly += sty;
+    }
+    return dth;
+}
+
 __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
 {
     return smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
@@ -159,10 +326,28 @@ __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
 
 // Persistent loop over tiles t = first, first + step, ... of a tile -> job map
 // (or of one job when `jobs` is null).  Buffer k & 1 holds tile k's footprint.
-template <int C>
+template <int C, int MODE = RO_FWD>
 __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, const MPJob *one, int total,
                                        int buf_floats, int *err)
 {
+    __shared__ float red[MP_RO_NT / 32];
+    // RO_DTH: this thread's running d theta share for job `cur`; flushed
+    // (block sum, one FP64 atomic) when the CTA moves to another job
+    const MPJob *cur = nullptr;
+    float dth = 0.f;
+    auto flush = [&]() {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dth += __shfl_down_sync(0xffffffffu, dth, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dth;
+        __syncthreads();
+        if (threadIdx.x == 0 && cur) {
+            float tot = 0.f;
+            for (int w = 0; w < MP_RO_NT / 32; ++w) tot += red[w];
+            atomicAdd(cur->acc, (double)tot);
+        }
+        __syncthreads();
+        dth = 0.f;
+    };
     extern __shared__ unsigned char mp_ro_smem[];
     unsigned char *base = ro_base(mp_ro_smem);
     uint64_t *bars = reinterpret_cast<uint64_t *>(base);
@@ -182,7 +367,7 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
             if (t >= total) break;
             const MPJob &J = job_of(t);
             if (!one) mp_tensormap_acquire(&J.tmap);
-            ro_issue<C>(J, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k, recs + k);
+            ro_issue<C, MODE>(J, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k, recs + k);
         }
     }
     int k = 0;
@@ -197,17 +382,29 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
             return;
         }
         const RoTile rec = recs[k & 1];
-        ro_tile<C>(J, rec, buf);
+        if (MODE == RO_FWD) {
+            ro_tile<C>(J, rec, buf);
+        } else if (MODE == RO_ADJ) {
+            ro_adj_tile<C>(J, rec, buf);
+        } else {
+            if (cur != &J) {
+                if (cur) flush();
+                cur = &J;
+            }
+            dth += ro_dth_tile<C>(J, rec, buf);
+        }
         __syncthreads();   // buffer and record k & 1 are free again
         if (threadIdx.x == 0) {
             const int tn = t + 2 * step;
             if (tn < total) {
                 const MPJob &Jn = job_of(tn);
                 if (!one) mp_tensormap_acquire(&Jn.tmap);
-                ro_issue<C>(Jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1), recs + (k & 1));
+                ro_issue<C, MODE>(Jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1),
+                                  recs + (k & 1));
             }
         }
     }
+    if (MODE == RO_DTH && cur) flush();
 }
 
 }  // namespace
@@ -229,15 +426,39 @@ MP_RO_KERNELS(mp_ro_c1, 1)
 MP_RO_KERNELS(mp_ro_c3, 3)
 MP_RO_KERNELS(mp_ro_c4, 4)
 
+// The adjoint's modes (batch launches only).
+#define MP_RO_MODE_KERNEL(NAME, C, MODE)                                                             \
+    __global__ void __launch_bounds__(MP_RO_NT) NAME(const MPJob *__restrict__ jobs,                 \
+                                                     const int *__restrict__ tile_job, int total,    \
+                                                     int buf_floats, int *err)                       \
+    {                                                                                               \
+        ro_run<C, MODE>(jobs, tile_job, nullptr, total, buf_floats, err);                            \
+    }
+
+MP_RO_MODE_KERNEL(mp_ro_adj_c1, 1, RO_ADJ)
+MP_RO_MODE_KERNEL(mp_ro_adj_c3, 3, RO_ADJ)
+MP_RO_MODE_KERNEL(mp_ro_adj_c4, 4, RO_ADJ)
+MP_RO_MODE_KERNEL(mp_ro_dth_c1, 1, RO_DTH)
+MP_RO_MODE_KERNEL(mp_ro_dth_c3, 3, RO_DTH)
+MP_RO_MODE_KERNEL(mp_ro_dth_c4, 4, RO_DTH)
+
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
+// Kernel of (mode, channel count); the adjoint's modes have batch kernels
+// only (c + 8 * mode selects them).
 static const void *mp_ro_fn(int c, bool single)
 {
     switch (c) {
     case 1: return single ? (const void *)mp_ro_c1_single : (const void *)mp_ro_c1_batch;
     case 3: return single ? (const void *)mp_ro_c3_single : (const void *)mp_ro_c3_batch;
     case 4: return single ? (const void *)mp_ro_c4_single : (const void *)mp_ro_c4_batch;
+    case 8 * RO_ADJ + 1: return single ? nullptr : (const void *)mp_ro_adj_c1;
+    case 8 * RO_ADJ + 3: return single ? nullptr : (const void *)mp_ro_adj_c3;
+    case 8 * RO_ADJ + 4: return single ? nullptr : (const void *)mp_ro_adj_c4;
+    case 8 * RO_DTH + 1: return single ? nullptr : (const void *)mp_ro_dth_c1;
+    case 8 * RO_DTH + 3: return single ? nullptr : (const void *)mp_ro_dth_c3;
+    case 8 * RO_DTH + 4: return single ? nullptr : (const void *)mp_ro_dth_c4;
     default: return nullptr;
     }
 }
@@ -253,6 +474,7 @@ MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
     if (e != cudaSuccess) return mp_cuda_status(e);
     for (int single = 0; single < 2; ++single) {
         const void *fn = mp_ro_fn(c, single != 0);
+        if (!fn && single && c >= 8) continue;   // adjoint modes: batch kernel only
         if (!fn) return MP_ERROR_UNSUPPORTED_TYPE;
         std::lock_guard<std::mutex> lk(mtx);
         bool have = false;
@@ -262,7 +484,11 @@ MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
         int optin = 0;
         e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (e != cudaSuccess) return mp_cuda_status(e);
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+        // the opt-in maximum covers static and dynamic shared memory together
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, fn);
+        if (e != cudaSuccess) return mp_cuda_status(e);
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
         if (e != cudaSuccess) return mp_cuda_status(e);
         done.push_back({fn, dev});
     }
