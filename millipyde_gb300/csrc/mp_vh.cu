@@ -63,7 +63,15 @@ static const void *mp_vh_fn(int code, bool single)
     }
 }
 
-int mp_vh_strip(int radius, int cm) { return 2 * MP_VH_NT - 2 * ((radius * cm + 3) & ~3); }
+// Threads of a code's kernels: the radius buckets run 256 per CTA.
+static int mp_vh_code_nt(int code) { return (code & 16) ? MP_VH_NT_BIG : MP_VH_NT; }
+
+// Strip width limit; radii above MP_VH_RMAX run on the bucket kernels.
+int mp_vh_strip(int radius, int cm)
+{
+    const int nt = radius > MP_VH_RMAX ? MP_VH_NT_BIG : MP_VH_NT;
+    return 2 * nt - 2 * ((radius * cm + 3) & ~3);
+}
 
 // Strip width in columns for an image of width w pixels (w * cm columns):
 // the fewest strips of at most mp_vh_strip(radius, cm) columns, evened out
@@ -79,7 +87,7 @@ int mp_vh_fit_strip(int radius, int w, int cm)
 
 size_t mp_vh_smem(int code)
 {
-    return (size_t)mp_vh::mp_vh_smem_floats(mp_vh_code_cin(code), mp_vh_code_cm(code)) * 4 + 128;
+    return (size_t)mp_vh::mp_vh_smem_floats(mp_vh_code_cin(code), mp_vh_code_cm(code), mp_vh_code_nt(code)) * 4 + 128;
 }
 
 MPStatus mp_vh_prepare(int code, int *ctas_per_sm)
@@ -106,7 +114,7 @@ MPStatus mp_vh_prepare(int code, int *ctas_per_sm)
         }
     }
     int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, MP_VH_NT, mp_vh_smem(code));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, mp_vh_code_nt(code), mp_vh_smem(code));
     if (e != cudaSuccess) return mp_cuda_status(e);
     if (n < 1) return MP_ERROR_TOO_LARGE;
     *ctas_per_sm = n;
@@ -122,7 +130,7 @@ MPStatus mp_vh_launch(int code, const MPJob *jobs_dev, const int *tile_job, int 
     if (grid > total) grid = total;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&total, (void *)&err, (void *)&counter};
-    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_VH_NT), args, mp_vh_smem(code), s));
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(mp_vh_code_nt(code)), args, mp_vh_smem(code), s));
 }
 
 MPStatus mp_vh_launch_single(int code, const MPJob &job, int grid, int *err, cudaStream_t s)
@@ -133,5 +141,5 @@ MPStatus mp_vh_launch_single(int code, const MPJob &job, int grid, int *err, cud
     if (grid > job.ntiles) grid = job.ntiles;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&job, (void *)&err};
-    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_VH_NT), args, mp_vh_smem(code), s));
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(mp_vh_code_nt(code)), args, mp_vh_smem(code), s));
 }

@@ -34,9 +34,9 @@
 #pragma once
 #include "mp_internal.cuh"
 
-#define MP_VH_NT 128
+#define MP_VH_NT 128       // threads of a CTA (2 columns each)
+#define MP_VH_NT_BIG 256   // threads of the radius-bucket kernels: wider strips, the halo a smaller share
 #define MP_VH_VR 8
-#define MP_VH_VW (2 * MP_VH_NT + 4)   // shared tile row stride (floats)
 
 namespace mp_vh {
 
@@ -108,9 +108,9 @@ __device__ __forceinline__ float2 prologue(const float *slot, bool in0, bool in1
 // horizontal tiles [2][VR][VW], two staging buffers [2][NW][VR][64*PX]
 // (PX = floats staged per column: CIN when CM = 1, else 1), then the 64
 // horizontal taps of the dot mode.
-__host__ __device__ constexpr int mp_vh_smem_floats(int cin, int cm)
+__host__ __device__ constexpr int mp_vh_smem_floats(int cin, int cm, int nt = MP_VH_NT)
 {
-    return 64 + 64 + 2 * MP_VH_VR * MP_VH_VW + 2 * MP_VH_VR * 2 * MP_VH_NT * (cm == 1 ? cin : 1) + 64;
+    return 64 + 64 + 2 * MP_VH_VR * (2 * nt + 4) + 2 * MP_VH_VR * 2 * nt * (cm == 1 ? cin : 1) + 64;
 }
 
 // Channel of interleaved float column f (f may be negative: halo columns).
@@ -134,11 +134,11 @@ __device__ __forceinline__ int chan_of(int f)
 // uses J.wts_h (the vertical pass J.wts), nothing is stored, and the sum of
 // output * J.aux (the output-space gradient) over the item is added to
 // J.acc[0] in FP64 (one atomic per warp and item).
-template <int CIN, int CM, int R, bool DOT = false>
+template <int CIN, int CM, int R, bool DOT = false, int NT = MP_VH_NT>
 __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32_t &gcount, int *err)
 {
     constexpr bool BIG = R > MP_VH_RMAX;
-    constexpr int NT = MP_VH_NT, VR = MP_VH_VR, VW = MP_VH_VW, NW = NT / 32;
+    constexpr int VR = MP_VH_VR, VW = 2 * NT + 4, NW = NT / 32;
     constexpr int NTAP = 2 * R + 1, RC = R * CM, R4 = (RC + 3) & ~3, E = R4 - RC;
     constexpr int NW2 = BIG ? R + 1 : NTAP;               // tap registers
     constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
@@ -469,9 +469,9 @@ __device__ __forceinline__ void vh_dispatch_dot(const MPJob &J, int lt, float *s
 template <int CIN, int CM>
 __device__ __forceinline__ void vh_dispatch_big(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
 {
-    if (J.radius <= 16) vh_item<CIN, CM, 16>(J, lt, smem, gc, err);
-    else if (J.radius <= 20) vh_item<CIN, CM, 20>(J, lt, smem, gc, err);
-    else if (J.radius <= MP_VH_RBIG) vh_item<CIN, CM, MP_VH_RBIG>(J, lt, smem, gc, err);
+    if (J.radius <= 16) vh_item<CIN, CM, 16, false, MP_VH_NT_BIG>(J, lt, smem, gc, err);
+    else if (J.radius <= 20) vh_item<CIN, CM, 20, false, MP_VH_NT_BIG>(J, lt, smem, gc, err);
+    else if (J.radius <= MP_VH_RBIG) vh_item<CIN, CM, MP_VH_RBIG, false, MP_VH_NT_BIG>(J, lt, smem, gc, err);
 }
 
 __device__ __forceinline__ float *vh_base(float4 *raw)
@@ -494,8 +494,8 @@ __device__ __forceinline__ void vh_init(float *smem)
 }  // namespace mp_vh
 
 // Persistent kernels: CTA b takes strip items b, b + grid, ...
-#define MP_VH_KERNELS_X(NAME, CIN, CM, DISPATCH, MINB)                                                                 \
-    __global__ void __launch_bounds__(MP_VH_NT, MINB) NAME##_batch(                                    \
+#define MP_VH_KERNELS_X(NAME, CIN, CM, DISPATCH, MINB, NTH)                                                                 \
+    __global__ void __launch_bounds__(NTH, MINB) NAME##_batch(                                    \
         const MPJob *__restrict__ jobs, const int *__restrict__ tile_job, int total, int *err,      \
         int *counter)                                                                               \
     {                                                                                               \
@@ -514,7 +514,7 @@ __device__ __forceinline__ void vh_init(float *smem)
             t = next_item;                                                                          \
         }                                                                                           \
     }                                                                                               \
-    __global__ void __launch_bounds__(MP_VH_NT, MINB)                                                  \
+    __global__ void __launch_bounds__(NTH, MINB)                                                  \
         NAME##_single(const __grid_constant__ MPJob job, int *err)                                  \
     {                                                                                               \
         extern __shared__ float4 mp_vh_dsmem4[];                                                    \
@@ -525,13 +525,14 @@ __device__ __forceinline__ void vh_init(float *smem)
             mp_vh::DISPATCH<CIN, CM>(job, t, smem, gc, err);                                         \
     }
 
-// Radii 1..MP_VH_RMAX and the d sigma dot mode (3 CTAs per SM; the dot
-// mode's second tap set costs a few spilled bytes at the largest radii), and
-// the buckets above MP_VH_RMAX (2 CTAs per SM: the larger window needs more
-// registers).
-#define MP_VH_KERNELS(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch, 3)
-#define MP_VH_KERNELS_BIG(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_big, 2)
+// Radii 1..MP_VH_RMAX and the d sigma dot mode (128 threads, 3 CTAs per SM;
+// the dot mode's second tap set costs a few spilled bytes at the largest
+// radii), and the buckets above MP_VH_RMAX (256 threads, 1 CTA per SM: the
+// larger window needs the registers, the wider strip keeps the halo share
+// down).
+#define MP_VH_KERNELS(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch, 3, MP_VH_NT)
+#define MP_VH_KERNELS_BIG(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_big, 1, MP_VH_NT_BIG)
 #ifndef MP_VH_DOT_MINB
 #define MP_VH_DOT_MINB 3
 #endif
-#define MP_VH_KERNELS_DOT(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_dot, MP_VH_DOT_MINB)
+#define MP_VH_KERNELS_DOT(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_dot, MP_VH_DOT_MINB, MP_VH_NT)
