@@ -92,6 +92,31 @@ __device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uin
     mp_tma_load_2d(buf, &J.tmap, bar, xf & ~3, by);
 }
 
+// Packed float pairs (one f32x2 instruction each).
+__device__ __forceinline__ float2 ro_fma2(float2 a, float2 b, float2 c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<unsigned long long *>(&a)), "l"(*reinterpret_cast<unsigned long long *>(&b)),
+          "l"(*reinterpret_cast<unsigned long long *>(&c)));
+    return *reinterpret_cast<float2 *>(&d);
+}
+
+__device__ __forceinline__ float2 ro_sub2(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<unsigned long long *>(&a)), "l"(*reinterpret_cast<unsigned long long *>(&b)));
+    return *reinterpret_cast<float2 *>(&d);
+}
+
+// Bilinear fraction of an 8.24 fixed-point coordinate from its top 23
+// fractional bits: 2^23 + f23 as a float bit pattern (exact), scaled on the
+// FMA pipe.
+__device__ __forceinline__ float ro_frac_bits(int l) { return __int_as_float(0x4B000000 | ((l >> 1) & 0x7FFFFF)); }
+
 // Epilogue kinds a tile is compiled for: none, one channel-preserving op of
 // a known kind, or a general list.
 enum { RO_EPI_NONE = 0, RO_EPI_GAMMA = 1, RO_EPI_BRIGHT = 2, RO_EPI_ONE = 3, RO_EPI_LIST = 4 };
@@ -128,6 +153,39 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
     float *drow = J.dst + (size_t)yf * dp + (size_t)xo * C;
     const size_t rstride = (size_t)RSTEP * dp;
     const bool full = y0 + TH <= ho;
+    if constexpr (C == 1 && (EK == RO_EPI_NONE || EK == RO_EPI_GAMMA || EK == RO_EPI_BRIGHT)) {
+        // one channel: two pixels (rows RSTEP apart) per step in packed
+        // pairs; lerp as a + f (b - a)
+        const float2 sc = make_float2(1.1920928955078125e-7f, 1.1920928955078125e-7f);
+        const float2 m1 = make_float2(-1.0f, -1.0f);
+#pragma unroll
+        for (int i = 0; i < NPX; i += 2) {
+            const int lxb = lx + stx, lyb = ly + sty;
+            const float2 fx = ro_fma2(make_float2(ro_frac_bits(lx), ro_frac_bits(lxb)), sc, m1);
+            const float2 fy = ro_fma2(make_float2(ro_frac_bits(ly), ro_frac_bits(lyb)), sc, m1);
+            const float *pa = buf + (ly >> 24) * bxw + (lx >> 24) + delta;
+            const float *pb = buf + (lyb >> 24) * bxw + (lxb >> 24) + delta;
+            const float2 a = make_float2(pa[0], pb[0]), b = make_float2(pa[1], pb[1]);
+            const float2 c = make_float2(pa[bxw], pb[bxw]), d = make_float2(pa[bxw + 1], pb[bxw + 1]);
+            const float2 v0 = ro_fma2(fx, ro_sub2(b, a), a);
+            const float2 v1 = ro_fma2(fx, ro_sub2(d, c), c);
+            const float2 v = ro_fma2(fy, ro_sub2(v1, v0), v0);
+            float o0 = v.x, o1 = v.y;
+            if (EK == RO_EPI_GAMMA) {
+                o0 = mp_clamp01(e1 * __powf(o0, e0));
+                o1 = mp_clamp01(e1 * __powf(o1, e0));
+            } else if (EK == RO_EPI_BRIGHT) {
+                o0 = mp_clamp01(o0 + e0);
+                o1 = mp_clamp01(o1 + e0);
+            }
+            if (full || yf + RSTEP * i < ho) drow[0] = o0;
+            if (full || yf + RSTEP * (i + 1) < ho) drow[rstride] = o1;
+            lx = lxb + stx;
+            ly = lyb + sty;
+            drow += 2 * rstride;
+        }
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < NPX; ++i) {
         if (full || yf + RSTEP * i < ho) {
