@@ -27,9 +27,11 @@
 //   V      a register window of 8 + 2R rows of (prologued) column pairs; each
 //          step produces 8 vertical outputs per column with packed f32x2
 //          FMAs, then slides the window by 8 rows.
-//   H      the 8 vertical rows go to a double-buffered shared tile; after one
-//          barrier every thread computes 8 consecutive horizontal outputs of
-//          one row from registers and applies the epilogue and fliplr map.
+//   H      the 8 vertical rows go to a double-buffered shared tile, rows 2p
+//          and 2p + 1 interleaved per column; after one barrier every thread
+//          computes 8 consecutive horizontal outputs of two rows at once
+//          (each tap one f32x2 FMA on a (row 2p, row 2p + 1) pair) and
+//          applies the epilogue and fliplr map.
 // The radius is a compile-time parameter (one instance per radius 1..12).
 #pragma once
 #include "mp_internal.cuh"
@@ -141,6 +143,9 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     constexpr int VR = MP_VH_VR, VW = 2 * NT + 4, NW = NT / 32;
     constexpr int NTAP = 2 * R + 1, RC = R * CM, R4 = (RC + 3) & ~3, E = R4 - RC;
     constexpr int NW2 = BIG ? R + 1 : NTAP;               // tap registers
+    // the plain one-channel family computes two output rows per
+    // horizontal work item as packed pairs
+    constexpr bool PAIR = CM == 1 && !BIG && !DOT;
     constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
     constexpr int D = R8 - R;                             // tap offset inside the window
     constexpr int NWIN = VR + 2 * R8;
@@ -294,11 +299,14 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
             if (tid == 0 && gB + 1 < ngroups) issue(gB + 1);   // buffer of group gB - 1, read last step
             alive = wait(gB);
             group_values(gB, win + 2 * R8);
-            float *tb = tile + (s & 1) * (VR * VW) + 2 * tid;
+            // PAIR: rows 2p and 2p + 1 interleaved per column (one float4 per
+            // row pair holds the thread's two columns of both rows); else
+            // row by row
+            float *tb = tile + (s & 1) * (VR * VW) + (PAIR ? 4 : 2) * tid;
+            float2 prev = make_float2(0.f, 0.f);
 #pragma unroll
             for (int o = 0; o < VR; ++o) {
                 float2 a = make_float2(0.f, 0.f);
-#pragma unroll
                 if constexpr (BIG) {
                     a = fma2(w2[R], win[o + D + R], a);
 #pragma unroll
@@ -307,12 +315,124 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
 #pragma unroll
                     for (int k = 0; k < NTAP; ++k) a = fma2(w2[k], win[o + D + k], a);
                 }
-                *reinterpret_cast<float2 *>(tb + o * VW) = a;
+                if constexpr (PAIR) {
+                    if (o & 1)
+                        *reinterpret_cast<float4 *>(tb + (o >> 1) * (2 * VW)) = make_float4(prev.x, a.x, prev.y, a.y);
+                    else
+                        prev = a;
+                } else {
+                    *reinterpret_cast<float2 *>(tb + o * VW) = a;
+                }
             }
 #pragma unroll
             for (int k = 0; k < 2 * R8; ++k) win[k] = win[k + VR];
         }
         if (s >= 1 && alive) {
+        if constexpr (PAIR) {
+            // ---- H: output rows of step s-1 from its shared tile, two rows
+            // per work item as packed pairs (one f32x2 FMA per tap for both)
+            const int sb = s - 1;
+            const float *tr = tile + (sb & 1) * (VR * VW);
+            for (int i = tid; i < (VR / 2) * ng; i += NT) {
+                const int rp = i & (VR / 2 - 1), g = i >> 2;
+                const int ya = y0 + VR * sb + 2 * rp;
+                const int xo0 = x0 + 8 * g;
+                if (ya >= y1 || xo0 >= W) continue;
+                const float *gp = tr + rp * (2 * VW) + 16 * g;   // column pairs from 8g on
+                float2 o2[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) o2[k] = make_float2(0.f, 0.f);
+                // consume the column pairs in order so that only the 8 sums
+                // stay live; taps CM columns apart (tap order per output)
+#pragma unroll
+                for (int q = 0; q < 2 * NLD; ++q) {
+                    const float4 v = ld4(gp + 4 * q);
+                    const float2 pc[2] = {make_float2(v.x, v.y), make_float2(v.z, v.w)};
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const int t = 2 * q + u - E - k;   // = m * CM for tap m
+                            if (t >= 0 && t % CM == 0 && t / CM < NTAP) {
+                                if constexpr (DOT) {
+                                    o2[k].x = fmaf(hw[t / CM], pc[u].x, o2[k].x);
+                                    o2[k].y = fmaf(hw[t / CM], pc[u].y, o2[k].y);
+                                } else {
+                                    const int m = t / CM;
+                                    o2[k] = fma2(w2[BIG ? (m <= R ? m : 2 * R - m) : m], pc[u], o2[k]);
+                                }
+                            }
+                        }
+                    }
+                }
+                // epilogue / store (or the dot product) of one output row
+                auto emit = [&](float (&o)[8], int y) {
+                    if constexpr (DOT) {
+                        const float *arow = J.aux + (size_t)y * J.aux_pitch;
+                        if (aux_vec && xo0 + 8 <= W) {
+                            const float4 p = ld4(arow + xo0), q = ld4(arow + xo0 + 4);
+                            dacc = fmaf(o[0], p.x, dacc);
+                            dacc = fmaf(o[1], p.y, dacc);
+                            dacc = fmaf(o[2], p.z, dacc);
+                            dacc = fmaf(o[3], p.w, dacc);
+                            dacc = fmaf(o[4], q.x, dacc);
+                            dacc = fmaf(o[5], q.y, dacc);
+                            dacc = fmaf(o[6], q.z, dacc);
+                            dacc = fmaf(o[7], q.w, dacc);
+                        } else {
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                if (xo0 + k < W) dacc = fmaf(o[k], arow[xo0 + k], dacc);
+                        }
+                        return;
+                    }
+                    if (epi.n) {
+                        if constexpr (CM == 1) {
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) o[k] = mp_pw_chan_f(epi, J.epi, o[k], 0, 1);
+                        } else {
+                            const int cb = xo0 % CM;
+                            int chv[8];
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) chv[k] = (cb + k) % CM;
+                            mp_pw_chan_n<8>(epi3, J.epi, o, chv, CM);
+                        }
+                    }
+                    float *drow = dst + (size_t)y * dp;
+                    if (vec && xo0 + 8 <= W) {
+                        *reinterpret_cast<float4 *>(drow + xo0) = make_float4(o[0], o[1], o[2], o[3]);
+                        *reinterpret_cast<float4 *>(drow + xo0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                    } else if constexpr (CM == 1) {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            if (xo0 + k < W) drow[flip ? wo - 1 - (xo0 + k) : xo0 + k] = o[k];
+                    } else if (CM == 4 && flip && J.vec_out && xo0 + 8 <= W) {
+                        // two whole pixels, mirrored: one float4 each
+                        const int px = xo0 >> 2;
+                        *reinterpret_cast<float4 *>(drow + (wo - 1 - px) * 4) = make_float4(o[0], o[1], o[2], o[3]);
+                        *reinterpret_cast<float4 *>(drow + (wo - 2 - px) * 4) = make_float4(o[4], o[5], o[6], o[7]);
+                    } else {
+                        // fliplr mirrors pixels and keeps the channel order
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const int f = xo0 + k;
+                            if (f < W) {
+                                const int px = f / CM, c = f - px * CM;
+                                drow[flip ? (wo - 1 - px) * CM + c : f] = o[k];
+                            }
+                        }
+                    }
+                };
+                float oa[8], ob[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    oa[k] = o2[k].x;
+                    ob[k] = o2[k].y;
+                }
+                emit(oa, ya);
+                if (ya + 1 < y1) emit(ob, ya + 1);
+            }
+        } else {
             // ---- H: output rows of step s-1 from its shared tile
             const int sb = s - 1;
             const float *tr = tile + (sb & 1) * (VR * VW);
@@ -418,6 +538,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                     }
                 }
             }
+        }
         }
         __syncthreads();
     }
