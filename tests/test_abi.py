@@ -129,3 +129,19 @@ def test_itemsize_table():
     L = _abi.lib()
     for t in (np.uint8, np.float32, np.float64, np.int64, np.int16):
         assert L.mp_type_itemsize(np.dtype(t).num) == np.dtype(t).itemsize
+
+
+def test_chain_backward_masked_host_checks():
+    # argument and descriptor checks happen on the host, before any device
+    # call: negative batch, missing buffers, unsupported channels, unknown ops
+    L = _abi.lib()
+    ops = (C.c_int * 2)(_abi.OP_ROTATE, _abi.OP_GAUSSIAN)
+    mask = (C.c_int * 2)(1, 0)
+    params = (C.c_double * 6)(10.0, 0, 0, 2.0, 0, 0)
+    f = L.mpk_chain_backward_masked
+    assert f(ops, 2, params, None, None, None, None, mask, -1, 8, 8, 3, None) == _abi.MP_ERROR_INVALID_ARGS
+    assert f(ops, 2, params, None, None, None, None, mask, 1, 8, 8, 3, None) == _abi.MP_ERROR_INVALID_ARGS
+    assert f(ops, 2, params, None, None, None, None, mask, 0, 8, 8, 2, None) == _abi.MP_ERROR_BAD_DESCRIPTOR
+    bad = (C.c_int * 1)(99)
+    assert f(bad, 1, params, None, None, None, None, mask, 0, 8, 8, 3, None) == _abi.MP_ERROR_BAD_DESCRIPTOR
+    assert f(ops, 2, params, None, None, None, None, mask, 0, 8, 8, 3, None) == _abi.MILLIPYDE_SUCCESS
