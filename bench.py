@@ -36,6 +36,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -113,7 +114,9 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "bench_clocks.csv")
+        # raw samples: $MP_BENCH_CLOCKS_CSV if set, else a per-process temp file
+        self.path = os.environ.get("MP_BENCH_CLOCKS_CSV") or os.path.join(
+            tempfile.gettempdir(), "mp_bench_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
