@@ -10,8 +10,9 @@
  * Everything is plain C: pointers, sizes and status codes.  No function
  * throws, none calls exit(); every failure is an MPStatus.  All entry points
  * are safe to call without the Python GIL and from several host threads
- * (there is no shared mutable device symbol: per-call parameters travel as
- * kernel arguments or in per-call device tables).
+ * (per-call parameters travel as kernel arguments or in per-call device
+ * tables; the one shared mutable device symbol is the scratch array and
+ * error word of mpk_pipeline_run_noalloc, whose overlapping calls race).
  *
  * Reference interfaces replaced (paths within jasbury1/millipyde):
  *   src/include/millipyde.h:16-126      MPObjData, MPStatus, MPFunc, arg structs
@@ -236,6 +237,23 @@ MPStatus mpdev_synchronize(void);
 /* Device name (e.g. "NVIDIA GB300") into buf (len bytes, NUL-terminated). */
 MPStatus mpdev_get_device_name(int device_id, char *buf, int len);
 MPStatus mpdev_stream_synchronize(void *stream);
+/* Reserved and in-use bytes of the device's stream-ordered memory pool (the
+ * pool every allocation of this library comes from), and the in-use high
+ * water mark since the last mpdev_pool_reset_peak (used_peak may be null). */
+MPStatus mpdev_pool_usage(int device_id, uint64_t *reserved, uint64_t *used, uint64_t *used_peak);
+MPStatus mpdev_pool_reset_peak(int device_id);
+/* Failure injection on the host: every later device allocation of the
+ * library larger than max_request_bytes fails with MP_ERROR_OUT_OF_MEMORY
+ * as if the device were full (0 removes the limit).  The reference exited
+ * the process on a failed hipMalloc (src/include/millipyde_hip_util.h:7-16);
+ * here the failing call returns the status and leaves its object as it was. */
+void mpdev_set_alloc_limit(size_t max_request_bytes);
+/* Self-test of the bounded device-side waits every kernel uses: one CTA
+ * waits on a barrier phase that never completes, gives up after `polls`
+ * polls (1 .. 2^21; about 1 us each after the first 2048) and reports it.
+ * Returns MP_ERROR_KERNEL_TIMEOUT with the device's error word cleared again,
+ * the context still usable. */
+MPStatus mpdev_selftest_wait_timeout(uint32_t polls, void *stream);
 
 /* ------------------------------------------------------------------------ */
 /* Batch pipeline: the fused, ragged path behind Pipeline.run and           */
@@ -343,7 +361,7 @@ MPStatus mpk_tune_get_gauss_tile(int cin, int cmid, int has_pro, int radius, int
  * after the prologue (1, 3 or 4). */
 MPStatus mpk_tune_set_stream(int cmid, int stages);
 /* Intermediate bytes one chunk of a fused batch may hold (at least 1 MB;
- * default 48 MB): a batch runs as one launch per segment per chunk. */
+ * default 512 MB): a batch runs as one launch per segment per chunk. */
 MPStatus mpk_tune_set_chunk_bytes(size_t bytes);
 void mpk_tune_clear(void);
 
@@ -378,10 +396,15 @@ MPStatus mpk_chain_backward_masked(const int *ops, int nops, const double *param
  * library holds until exit; any image whose intermediate would exceed 16 MB
  * is rejected with MP_ERROR_TOO_LARGE before anything is launched.  Images
  * run one after another on `stream`; the call returns when they are done.
+ * Every image is validated (descriptors, parameters, intermediate sizes)
+ * before the first launch, so a rejected call leaves every output untouched.
  * Its first call on a device resolves the array's device address (set-up,
- * with that device current).  Every call uses the same array, so calls that
- * overlap on the GPU (other threads or streams) race; stale contents from an
- * earlier call are never read. */
+ * with that device current; make that first call before any stream capture);
+ * the address is kept for the life of the process, so cudaDeviceReset ends
+ * this entry point's use in that process.  Every call uses the same array and
+ * error word, so calls that overlap on the GPU (other threads or streams)
+ * race; each call clears the error word before its first launch, and stale
+ * array contents from an earlier call are never read. */
 MPStatus mpk_pipeline_run_noalloc(const MPStage *stages, int nstages, const MPImage *in,
                                   const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
                                   void *stream);

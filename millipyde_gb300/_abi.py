@@ -108,6 +108,10 @@ SIGNATURES = {
     "mpdev_synchronize": (_ST, []),
     "mpdev_get_device_name": (_ST, [C.c_int, C.c_char_p, C.c_int]),
     "mpdev_stream_synchronize": (_ST, [_P]),
+    "mpdev_pool_usage": (_ST, [C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "mpdev_pool_reset_peak": (_ST, [C.c_int]),
+    "mpdev_set_alloc_limit": (None, [C.c_size_t]),
+    "mpdev_selftest_wait_timeout": (_ST, [C.c_uint32, _P]),
     "mpk_pipeline_shapes": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
                                   C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64]),
     "mpk_pipeline_run": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),

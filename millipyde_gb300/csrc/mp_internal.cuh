@@ -349,12 +349,13 @@ __device__ __forceinline__ bool mp_mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: returns false if the phase did not complete within
-// MP_SPIN_LIMIT polls (about two seconds), so a lost transfer turns into an
+// Bounded wait: returns false if the phase did not complete within `limit`
+// polls (MP_SPIN_LIMIT: about two seconds), so a lost transfer turns into an
 // error status instead of a hung GPU.
-__device__ __forceinline__ bool mp_mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ bool mp_mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                     uint32_t limit = MP_SPIN_LIMIT)
 {
-    for (uint32_t i = 0; i < MP_SPIN_LIMIT; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         if (mp_mbar_try_wait(bar, parity)) return true;
         if (i >= MP_SPIN_FAST) __nanosleep(1000);
     }
@@ -429,10 +430,12 @@ MPStatus mp_launch_adjoint(int kind, const MPJob *jobs_dev, const int *tile_job,
 // Single-job launch with an explicit device error word (no allocation).
 MPStatus mp_launch_single_err(int kind, const MPJob &job, size_t smem_bytes, int *err, cudaStream_t s);
 // Runs the stages on one image, intermediates in the two caller-provided
-// device buffers of half_bytes each; allocates no device memory.
+// device buffers of half_bytes each; allocates no device memory.  With
+// launch = false it only validates (descriptors, parameters, intermediate
+// sizes) and launches nothing.
 MPStatus mp_run_image_noalloc(const MPStage *stages, int nstages, uint64_t seed, uint64_t index,
                               const MPImage &in, const MPImage &out, void *half0, void *half1,
-                              size_t half_bytes, int *err, cudaStream_t s);
+                              size_t half_bytes, int *err, cudaStream_t s, bool launch);
 // The reference's own layouts (uint8 RGBA / uint8 RGB for rgb2grey /
 // float64 greyscale) and arithmetic, in place on an object (mp_legacy.cu).
 MPStatus mp_legacy_apply(MPObjData *o, int op, double p0, double p1, double p2);

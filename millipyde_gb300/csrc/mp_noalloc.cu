@@ -12,7 +12,11 @@
 // The array costs MP_NOALLOC_SCRATCH_BYTES on every GPU that loads the
 // library, for the life of the process.  In host code its name is only a
 // host-side stand-in: the device address is looked up once per device with
-// cudaGetSymbolAddress (with that device current) and passed to the kernels.
+// cudaGetSymbolAddress (with that device current, on the first call on that
+// device) and passed to the kernels.  The address is kept for the life of
+// the process, so a process that calls cudaDeviceReset (which unloads the
+// library's device image) must not use this entry point afterwards.  The
+// first call on a device should come before any stream capture.
 #include <mutex>
 #include <string.h>
 
@@ -60,6 +64,27 @@ static MPStatus mp_noalloc_setup(int dev, MPNoallocDevice *out)
     return MILLIPYDE_SUCCESS;
 }
 
+// Stream-ordered read of this call's error word after its launches, then
+// wait for the stream; a set word becomes MP_ERROR_KERNEL_TIMEOUT and is
+// cleared.  Runs on every exit path after the first launch, so the call
+// never returns with its work still in flight on the caller's buffers.
+static MPStatus mp_noalloc_finish(const MPNoallocDevice &d, cudaStream_t s, MPStatus launch_status)
+{
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, d.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    const cudaError_t es = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = es;
+    if (launch_status != MILLIPYDE_SUCCESS) return launch_status;
+    if (e != cudaSuccess) return mp_cuda_status(e);
+    if (h != MP_KERR_NONE) {
+        e = cudaMemsetAsync(d.err, 0, sizeof(int), s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return mp_cuda_status(e);
+        return MP_ERROR_KERNEL_TIMEOUT;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
 extern "C" MPStatus mpk_pipeline_run_noalloc(const MPStage *stages, int nstages, const MPImage *in,
                                              const MPImage *out, int nimgs, uint64_t seed,
                                              uint64_t index0, void *stream)
@@ -73,23 +98,22 @@ extern "C" MPStatus mpk_pipeline_run_noalloc(const MPStage *stages, int nstages,
     MPStatus st = mp_noalloc_setup(dev, &d);
     if (st != MILLIPYDE_SUCCESS) return st;
     cudaStream_t s = (cudaStream_t)stream;
+    // 1. validate every image (descriptors, parameters, intermediate sizes)
+    //    before anything is launched
     for (int i = 0; i < nimgs; ++i) {
-        st = mp_run_image_noalloc(stages, nstages, seed, index0 + (uint64_t)i, in[i], out[i],
-                                  d.scratch, d.scratch + MP_NOALLOC_HALF_BYTES,
-                                  MP_NOALLOC_HALF_BYTES, d.err, s);
+        st = mp_run_image_noalloc(stages, nstages, seed, index0 + (uint64_t)i, in[i], out[i], d.scratch,
+                                  d.scratch + MP_NOALLOC_HALF_BYTES, MP_NOALLOC_HALF_BYTES, d.err, s, false);
         if (st != MILLIPYDE_SUCCESS) return st;
     }
-    // The call returns after its work is done, reporting a timed-out
-    // device-side wait (and clearing the word for the next call).
-    int h = 0;
-    e = cudaMemcpyFromSymbolAsync(&h, mp_noalloc_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (nimgs == 0) return MILLIPYDE_SUCCESS;
+    // 2. the error word starts at zero for this call: a word left set by an
+    //    earlier call (or another caller) is not reported here
+    e = cudaMemsetAsync(d.err, 0, sizeof(int), s);
     if (e != cudaSuccess) return mp_cuda_status(e);
-    if (h != MP_KERR_NONE) {
-        const int zero = 0;
-        cudaMemcpyToSymbolAsync(mp_noalloc_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s);
-        cudaStreamSynchronize(s);
-        return MP_ERROR_KERNEL_TIMEOUT;
-    }
-    return MILLIPYDE_SUCCESS;
+    // 3. images one after another, intermediates in the two halves
+    for (int i = 0; i < nimgs && st == MILLIPYDE_SUCCESS; ++i)
+        st = mp_run_image_noalloc(stages, nstages, seed, index0 + (uint64_t)i, in[i], out[i], d.scratch,
+                                  d.scratch + MP_NOALLOC_HALF_BYTES, MP_NOALLOC_HALF_BYTES, d.err, s, true);
+    // 4. wait for the work, report a timed-out device-side wait
+    return mp_noalloc_finish(d, s, st);
 }

@@ -2206,7 +2206,7 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
 // ---------------------------------------------------------------------------
 MPStatus mp_run_image_noalloc(const MPStage *stages, int nstages, uint64_t seed, uint64_t index,
                               const MPImage &in, const MPImage &out, void *half0, void *half1,
-                              size_t half_bytes, int *err, cudaStream_t s)
+                              size_t half_bytes, int *err, cudaStream_t s, bool launch)
 {
     if (in.channels != 1 && in.channels != 3 && in.channels != 4) return MP_ERROR_BAD_DESCRIPTOR;
     if (in.height < 0 || in.width < 0 || (in.pitch % 4) ||
@@ -2227,6 +2227,7 @@ MPStatus mp_run_image_noalloc(const MPStage *stages, int nstages, uint64_t seed,
         const size_t need = (size_t)segs[k].hout * mp_round16((long long)segs[k].wout * segs[k].cout * 4);
         if (need > half_bytes) return MP_ERROR_TOO_LARGE;
     }
+    if (!launch) return MILLIPYDE_SUCCESS;
     MPImage cur = in;
     for (size_t k = 0; k < segs.size(); ++k) {
         MPImage dst;

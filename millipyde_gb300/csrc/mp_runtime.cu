@@ -258,11 +258,79 @@ extern "C" MPStatus mpdev_stream_synchronize(void *stream)
     return MILLIPYDE_SUCCESS;
 }
 
+// Largest single device allocation the library makes (0: no limit); set by
+// mpdev_set_alloc_limit to exercise the out-of-memory paths on the host.
+static std::atomic<size_t> mp_alloc_limit{0};
+
+extern "C" void mpdev_set_alloc_limit(size_t max_request_bytes) { mp_alloc_limit.store(max_request_bytes); }
+
 MPStatus mp_malloc_async(void **p, size_t bytes, cudaStream_t s)
 {
     *p = nullptr;
     if (bytes == 0) return MILLIPYDE_SUCCESS;
+    const size_t lim = mp_alloc_limit.load();
+    if (lim && bytes > lim) return MP_ERROR_OUT_OF_MEMORY;
     return mp_cuda_status(cudaMallocAsync(p, bytes, s));
+}
+
+extern "C" MPStatus mpdev_pool_usage(int device_id, uint64_t *reserved, uint64_t *used, uint64_t *used_peak)
+{
+    if (!reserved || !used) return MP_ERROR_INVALID_ARGS;
+    if (!mpdev_is_valid_device(device_id)) return MP_ERROR_NO_DEVICE;
+    cudaMemPool_t pool;
+    MP_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, device_id));
+    cuuint64_t r = 0, u = 0, h = 0;
+    MP_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r));
+    MP_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u));
+    MP_CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &h));
+    *reserved = (uint64_t)r;
+    *used = (uint64_t)u;
+    if (used_peak) *used_peak = (uint64_t)h;
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpdev_pool_reset_peak(int device_id)
+{
+    if (!mpdev_is_valid_device(device_id)) return MP_ERROR_NO_DEVICE;
+    cudaMemPool_t pool;
+    MP_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, device_id));
+    cuuint64_t zero = 0;
+    MP_CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+    return MILLIPYDE_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Self-test of the bounded device-side wait: one CTA waits on an mbarrier
+// phase that never completes (two arrivals expected, one made; no copy is
+// involved), gives up after `polls` polls through the same wait the kernels
+// use, and reports MP_KERR_TIMEOUT into the device's error word.
+// ---------------------------------------------------------------------------
+__global__ void mp_selftest_wait_kernel(int *err, uint32_t polls)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mp_mbar_init(&bar, 2);
+        mp_fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mp_smem_addr(&bar)) : "memory");
+    }
+    const bool ok = mp_mbar_wait_bounded(&bar, 0, polls);
+    if (!__syncthreads_and(ok) && threadIdx.x == 0) atomicExch(err, MP_KERR_TIMEOUT);
+}
+
+extern "C" MPStatus mpdev_selftest_wait_timeout(uint32_t polls, void *stream)
+{
+    int d = 0;
+    MP_CUDA_TRY(cudaGetDevice(&d));
+    int *w = mp_device_error_word(d);
+    if (!w) return MP_ERROR_NO_DEVICE;
+    if (polls == 0 || polls > MP_SPIN_LIMIT) return MP_ERROR_INVALID_ARGS;
+    cudaStream_t s = (cudaStream_t)stream;
+    mp_selftest_wait_kernel<<<1, 32, 0, s>>>(w, polls);
+    MP_CUDA_TRY(cudaGetLastError());
+    return mp_check_device_error(s);
 }
 
 void mp_free_async(void *p, cudaStream_t s)

@@ -150,6 +150,52 @@ def rotate(img, angle, mode="bilinear"):
     return (1 - fy) * ((1 - fx) * a + fx * b) + fy * ((1 - fx) * c + fx * d)
 
 
+def gaussian_rotate_window(img, sigma, angle, rows, cols):
+    """Output pixels [rows[0]:rows[1], cols[0]:cols[1]] of
+    rotate(gaussian(img, sigma), angle), computed from the source rows and
+    columns that window needs only (for images too large for the whole-image
+    oracle).  Same formulas as gaussian() and rotate(): the blur is evaluated
+    on the bounding box of the window's bilinear neighbours, from a source
+    crop r pixels wider on every side that is not an image edge, so zero
+    padding applies only at the real image edges
+    (src/millipyde_image.cpp:170-172, :114-139)."""
+    x = img    # only the crop below is read: any array with .shape, .ndim and 2-D slicing
+    h, w = x.shape[0], x.shape[1]
+    chan = x.shape[2:] if x.ndim == 3 else ()
+    th = angle * DEG2RAD
+    c, s = math.cos(th), math.sin(th)
+    ys, xs = np.meshgrid(np.arange(rows[0], rows[1], dtype=np.float64),
+                         np.arange(cols[0], cols[1], dtype=np.float64), indexing="ij")
+    dx, dy = xs - w / 2.0, ys - h / 2.0
+    sx, sy = c * dx - s * dy + w / 2.0, s * dx + c * dy + h / 2.0
+    x0, y0 = np.floor(sx).astype(np.int64), np.floor(sy).astype(np.int64)
+    fx, fy = sx - x0, sy - y0
+    out_shape = sx.shape + chan
+    # bounding box (inside the image) of every neighbour the window reads
+    bx0, bx1 = max(0, int(x0.min())), min(w - 1, int(x0.max()) + 1)
+    by0, by1 = max(0, int(y0.min())), min(h - 1, int(y0.max()) + 1)
+    if bx0 > bx1 or by0 > by1:
+        return np.zeros(out_shape)
+    r = gaussian_radius(sigma)
+    cx0, cx1 = max(0, bx0 - r), min(w - 1, bx1 + r)
+    cy0, cy1 = max(0, by0 - r), min(h - 1, by1 + r)
+    crop = _f64(np.asarray(x[cy0:cy1 + 1, cx0:cx1 + 1]))
+    wts = gaussian_weights(sigma, r)
+    blur = _correlate_axis(_correlate_axis(crop, wts, 1), wts, 0)
+
+    def tap(ix, iy):
+        ok = (ix >= 0) & (ix < w) & (iy >= 0) & (iy < h)
+        v = np.zeros(out_shape)
+        v[ok] = blur[iy[ok] - cy0, ix[ok] - cx0]
+        return v
+
+    a, b = tap(x0, y0), tap(x0 + 1, y0)
+    cc, d = tap(x0, y0 + 1), tap(x0 + 1, y0 + 1)
+    if chan:
+        fx, fy = fx[..., None], fy[..., None]
+    return (1 - fy) * ((1 - fx) * a + fx * b) + fy * ((1 - fx) * cc + fx * d)
+
+
 def brightness(img, delta):
     """clamp01(x + delta) on colour channels  (src/millipyde_image.cpp:384-398)."""
     col, alpha = _split_alpha(_f64(img))

@@ -7,7 +7,7 @@ reference on small seeded inputs -- uint8 RGBA images and float64 greyscale
 images, the two layouts the reference handles -- and stores inputs, op
 parameters and outputs.  Run here, where the reference checkout exists:
 
-    python oracle/ref_golden.py [--reference /root/reference]
+    python oracle/ref_golden.py --reference <path of the reference checkout>
 
 The .npz is committed; tests read it without the reference.
 """
@@ -92,7 +92,7 @@ def cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="path of the reference checkout")
     args = ap.parse_args()
     lib = build(args.reference)
     blob = {}

@@ -1,0 +1,94 @@
+"""GPU parity at the benchmark configurations' own sizes.
+
+The smaller parity tests use images of a few hundred pixels; these cases
+reach the sizes the benchmarks run:
+  - the ragged augmentation batch with its extreme shapes (2048 x 2048,
+    2048 x 64, 64 x 2048, 1500 x 37, 37 x 1500 RGB) and its random stages:
+    multi-strip rows of the channel-preserving gaussian and the rotate's
+    widest footprints;
+  - four whole 1024 x 1024 images of the uniform batch;
+  - one 8192 x 8192 x 3 image of the large-image chain (gaussian sigma 8,
+    radius 24 -> rotate 37 deg -> brightness), compared on windows of the
+    output (corners, centre, last rows and columns) with an oracle that reads
+    only the source region each window needs.
+Every float result is held to max-abs 1e-5 against the FP64 oracle.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from millipyde_gb300 import _abi
+from oracle import oracle as O
+
+from helpers import TOL, maxabs
+from test_pipeline_gpu import check_spec
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+RAGGED = [dict(op="rotate", random=True, lo=(-45,), hi=(45,)),
+          dict(op="gaussian", random=True, lo=(0.5,), hi=(4.0,)),
+          dict(op="adjust_gamma", random=True, lo=(0.5, 1.0), hi=(2.0, 1.0)),
+          dict(op="brightness", random=True, lo=(-0.2,), hi=(0.2,)),
+          dict(op="fliplr", probability=0.5)]
+
+
+def test_ragged_batch_extreme_shapes(gpu):
+    rng = np.random.default_rng(21)
+    shapes = [(2048, 2048), (2048, 64), (64, 2048), (1500, 37), (37, 1500), (64, 64), (777, 1999)]
+    xs = [rng.random((h, w, 3), dtype=np.float32) for h, w in shapes]
+    # two seeds: different angles, radii and flips for every shape
+    for seed in (3, 8):
+        check_spec(RAGGED, xs, seed=seed, index0=0)
+
+
+def test_uniform_batch_whole_images(gpu):
+    rng = np.random.default_rng(22)
+    spec = [dict(op="rgb2grey"), dict(op="gaussian", lo=(3.0,)), dict(op="rotate", lo=(17.0,)),
+            dict(op="adjust_gamma", lo=(0.8, 1.0))]
+    xs = [rng.random((1024, 1024, 3), dtype=np.float32) for _ in range(4)]
+    check_spec(spec, xs)
+
+
+def test_large_image_chain_8192(gpu):
+    """16 x 8192^2 RGB is the benchmark; one image is enough for parity: the
+    kernels see the same row length, radius-24 bucket and rotated
+    footprints."""
+    L = _abi.lib()
+    H = W = 8192
+    sigma, angle, delta = 8.0, 37.0, 0.05
+    g = torch.Generator(device="cuda")
+    g.manual_seed(23)
+    x = torch.rand((H, W * 3), device="cuda", generator=g)
+    y = torch.full((H, W * 3), float("nan"), device="cuda")
+    st = _abi.stages(_abi.stage("gaussian", sigma), _abi.stage("rotate", angle), _abi.stage("brightness", delta))
+    ins = _abi.images([_abi.image(x.data_ptr(), H, W, 3, W * 12)])
+    outs = _abi.images([_abi.image(y.data_ptr(), H, W, 3, W * 12)])
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _abi.check(L.mpk_pipeline_run(st, 3, ins, outs, 1, 0, 0, stream))
+    # the autograd path's forward (dense batch entry) on the same image
+    y2 = torch.full((H, W * 3), float("nan"), device="cuda")
+    ops = (C.c_int * 3)(_abi.OP_GAUSSIAN, _abi.OP_ROTATE, _abi.OP_BRIGHTNESS)
+    params = (C.c_double * 9)(sigma, 0, 0, angle, 0, 0, delta, 0, 0)
+    _abi.check(L.mpk_chain_forward(ops, 3, C.cast(params, C.c_void_p), C.c_void_p(x.data_ptr()),
+                                   C.c_void_p(y2.data_ptr()), 1, H, W, 3, stream))
+    torch.cuda.synchronize()
+
+    class DeviceImage:
+        """The device input, read crop by crop by the windowed oracle."""
+        shape, ndim = (H, W, 3), 3
+
+        def __getitem__(self, idx):
+            return x.view(H, W, 3)[idx].cpu().numpy()
+
+    xv = DeviceImage()
+    windows = [((0, 48), (0, 64)), ((4064, 4128), (4064, 4160)), ((H - 40, H), (W - 72, W)),
+               ((0, 32), (W - 96, W)), ((H - 64, H), (0, 80)), ((1000, 1024), (7000, 7168))]
+    for rows, cols in windows:
+        ref = O.brightness(O.gaussian_rotate_window(xv, sigma, angle, rows, cols), delta)
+        got = y.view(H, W, 3)[rows[0]:rows[1], cols[0]:cols[1]].cpu().numpy()
+        got2 = y2.view(H, W, 3)[rows[0]:rows[1], cols[0]:cols[1]].cpu().numpy()
+        assert maxabs(got, ref) <= TOL, (rows, cols)
+        assert maxabs(got2, ref) <= TOL, (rows, cols)
+    assert not bool(torch.isnan(y).any()) and not bool(torch.isnan(y2).any())

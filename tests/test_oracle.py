@@ -105,3 +105,17 @@ def test_counter_uniform_range_and_determinism():
     assert abs(np.mean(u) - 0.5) < 0.03
     assert u == [O.counter_uniform(7, i, 2, 1) for i in range(2000)]
     assert O.counter_uniform(7, 0, 2, 1) != O.counter_uniform(8, 0, 2, 1)
+
+
+def test_gaussian_rotate_window_equals_whole_image():
+    """The windowed oracle (used for the 8192^2 parity case) reproduces the
+    whole-image oracle on every window, edges and corners included."""
+    rng = np.random.default_rng(5)
+    for shape, sigma, angle in [((150, 170, 3), 2.0, 37.0), ((97, 61), 1.2, -44.0), ((64, 200, 3), 4.0, 90.0)]:
+        x = rng.random(shape)
+        full = O.rotate(O.gaussian(x, sigma), angle)
+        h, w = shape[:2]
+        for rows, cols in [((0, 20), (0, 30)), ((h // 3, h // 2), (w // 4, w // 2)), ((h - 9, h), (w - 13, w)),
+                           ((0, h), (w - 3, w))]:
+            win = O.gaussian_rotate_window(x, sigma, angle, rows, cols)
+            assert np.abs(win - full[rows[0]:rows[1], cols[0]:cols[1]]).max() <= 1e-12
