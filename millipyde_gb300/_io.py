@@ -2,8 +2,9 @@
 
 The reference read files with scikit-image (src/gpuimage.c:574-688), which is
 not a dependency here.  This module decodes PNG with the standard library
-(zlib): 8- and 16-bit greyscale, grey+alpha, RGB and RGBA, non-interlaced,
-all five row filters.  Results are uint8 (or uint16) arrays of shape (H, W)
+(zlib) with the row filters reversed in C (the extension's _png_unfilter):
+8- and 16-bit greyscale, grey+alpha, RGB and RGBA, non-interlaced, all
+five row filters.  Results are uint8 (or uint16) arrays of shape (H, W)
 or (H, W, C), as skimage.io.imread returns them.  Directory listings are
 sorted by file name (the reference used readdir order, which depends on the
 filesystem).
@@ -47,36 +48,11 @@ def read_png(path: str) -> np.ndarray:
     ch = _CHANNELS[color]
     bpp = ch * depth // 8
     stride = w * bpp
-    raw = np.frombuffer(zlib.decompress(b"".join(idat)), dtype=np.uint8)
-    raw = raw[: h * (stride + 1)].reshape(h, stride + 1)
-    out = np.zeros((h, stride), dtype=np.int32)
-    prev = np.zeros(stride, dtype=np.int32)
-    for y in range(h):
-        ft = raw[y, 0]
-        line = raw[y, 1:].astype(np.int32)
-        if ft == 0:
-            cur = line
-        elif ft == 2:
-            cur = (line + prev) & 0xFF
-        else:
-            cur = np.empty(stride, dtype=np.int32)
-            for x in range(stride):  # sequential dependency on the left neighbour
-                left = cur[x - bpp] if x >= bpp else 0
-                up = prev[x]
-                ul = prev[x - bpp] if x >= bpp else 0
-                if ft == 1:
-                    v = line[x] + left
-                elif ft == 3:
-                    v = line[x] + ((left + up) >> 1)
-                else:
-                    p = left + up - ul
-                    pa, pb, pc = abs(p - left), abs(p - up), abs(p - ul)
-                    v = line[x] + (left if (pa <= pb and pa <= pc) else (up if pb <= pc else ul))
-                cur[x] = v & 0xFF
-        out[y] = cur
-        prev = cur
+    from ._millipyde import _png_unfilter
+    out = np.frombuffer(_png_unfilter(zlib.decompress(b"".join(idat)), h, stride, bpp), dtype=np.uint8)
+    out = out.reshape(h, stride)
     if depth == 8:
-        img = out.astype(np.uint8).reshape(h, w, ch)
+        img = out.reshape(h, w, ch).copy()
     else:
         b = out.astype(np.uint16).reshape(h, w * ch, 2)
         img = ((b[..., 0] << 8) | b[..., 1]).reshape(h, w, ch)

@@ -1240,13 +1240,33 @@ MPStatus mpk_pipeline_run(const MPStage *stages, int nstages, const MPImage *in,
 
 }  // extern "C"
 
-// Plain per-op path: one launch per stage and image, a fresh pool buffer per
-// stage (what the reference's Pipeline did, minus its per-stage host sync).
-static MPStatus mp_run_ops_unfused(const std::vector<ROp> &ops, const MPImage &in,
-                                   const MPImage &out, cudaStream_t s)
+// Plain per-op path: one launch per stage and image, each stage's result in
+// device memory (what the reference's Pipeline did, minus its per-stage host
+// sync and per-stage allocation).  Intermediates alternate between two
+// buffers allocated once per batch (sized for the largest intermediate), so
+// the baseline pays the per-op kernels' memory traffic and launches, not
+// allocator calls.
+static size_t mp_unfused_inter_bytes(const std::vector<ROp> &ops, const MPImage &in)
+{
+    size_t need = 0;
+    int h = in.height, w = in.width, c = in.channels;
+    for (size_t k = 0; k + 1 < ops.size(); ++k) {
+        std::vector<ROp> one(1, ops[k]);
+        std::vector<Seg> sg;
+        mp_segment(one, c, h, w, sg);
+        const Seg &g = sg.back();
+        h = g.hout;
+        w = g.wout;
+        c = g.cout;
+        need = std::max(need, (size_t)h * mp_round16((long long)w * c * 4));
+    }
+    return need;
+}
+
+static MPStatus mp_run_ops_unfused(const std::vector<ROp> &ops, const MPImage &in, const MPImage &out,
+                                   void *const bufs[2], cudaStream_t s)
 {
     MPImage cur = in;
-    void *owned = nullptr;
     if (ops.empty()) {
         std::vector<Seg> sg;
         mp_segment(ops, in.channels, in.height, in.width, sg);
@@ -1258,7 +1278,6 @@ static MPStatus mp_run_ops_unfused(const std::vector<ROp> &ops, const MPImage &i
         mp_segment(one, cur.channels, cur.height, cur.width, sg);
         const Seg &g = sg.back();
         MPImage nx;
-        void *buf = nullptr;
         if (k + 1 == ops.size()) {
             nx = out;
         } else {
@@ -1266,14 +1285,10 @@ static MPStatus mp_run_ops_unfused(const std::vector<ROp> &ops, const MPImage &i
             nx.width = g.wout;
             nx.channels = g.cout;
             nx.pitch = mp_round16((long long)nx.width * nx.channels * 4);
-            MPStatus st = mp_malloc_async(&buf, (size_t)nx.height * nx.pitch, s);
-            if (st != MILLIPYDE_SUCCESS) { mp_free_async(owned, s); return st; }
-            nx.data = buf;
+            nx.data = bufs[k & 1];
         }
         MPStatus st = mp_run_segment_single(g, cur, nx, s);
-        mp_free_async(owned, s);
-        owned = buf;
-        if (st != MILLIPYDE_SUCCESS) { mp_free_async(owned, s); return st; }
+        if (st != MILLIPYDE_SUCCESS) return st;
         cur = nx;
     }
     return MILLIPYDE_SUCCESS;
@@ -1284,14 +1299,21 @@ extern "C" MPStatus mpk_pipeline_run_unfused(const MPStage *stages, int nstages,
                                              uint64_t index0, void *stream)
 {
     if (nimgs < 0 || nstages < 0 || (nimgs > 0 && (!in || !out))) return MP_ERROR_INVALID_ARGS;
-    std::vector<ROp> ops;
+    cudaStream_t s = (cudaStream_t)stream;
+    std::vector<std::vector<ROp>> all(nimgs);
+    size_t need = 0;
     for (int i = 0; i < nimgs; ++i) {
-        MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, ops, nullptr);
+        MPStatus st = mp_resolve_image(stages, nstages, seed, index0 + (uint64_t)i, all[i], nullptr);
         if (st != MILLIPYDE_SUCCESS) return st;
-        st = mp_run_ops_unfused(ops, in[i], out[i], (cudaStream_t)stream);
-        if (st != MILLIPYDE_SUCCESS) return st;
+        need = std::max(need, mp_unfused_inter_bytes(all[i], in[i]));
     }
-    return MILLIPYDE_SUCCESS;
+    void *bufs[2] = {nullptr, nullptr};
+    MPStatus st = mp_malloc_async(&bufs[0], need, s);
+    if (st == MILLIPYDE_SUCCESS) st = mp_malloc_async(&bufs[1], need, s);
+    for (int i = 0; i < nimgs && st == MILLIPYDE_SUCCESS; ++i) st = mp_run_ops_unfused(all[i], in[i], out[i], bufs, s);
+    mp_free_async(bufs[0], s);
+    mp_free_async(bufs[1], s);
+    return st;
 }
 
 // ---------------------------------------------------------------------------

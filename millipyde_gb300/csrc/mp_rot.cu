@@ -451,7 +451,12 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
             }
             dth += ro_dth_tile<C>(J, rec, buf);
         }
-        __syncthreads();   // buffer and record k & 1 are free again
+        // buffer and record k & 1 are free again.  The d theta sum lives in a
+        // register: the barrier's predicate depends on it, so this tile's
+        // shared-memory loads have completed before the buffer is refilled by
+        // TMA (the forward and dx modes store their results first).
+        if (MODE == RO_DTH) __syncthreads_or(dth == 3.0e38f);
+        else __syncthreads();
         if (threadIdx.x == 0) {
             const int tn = t + 2 * step;
             if (tn < total) {

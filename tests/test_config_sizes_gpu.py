@@ -92,3 +92,19 @@ def test_large_image_chain_8192(gpu):
         assert maxabs(got, ref) <= TOL, (rows, cols)
         assert maxabs(got2, ref) <= TOL, (rows, cols)
     assert not bool(torch.isnan(y).any()) and not bool(torch.isnan(y2).any())
+
+
+def test_streaming_gaussian_mirrored_wide_rows_repeated(gpu):
+    """The streaming gaussian's window head keeps staged rows in registers
+    across barriers while the staging buffer is refilled; mirrored RGB
+    output (eight scalar stores per group) on a 1999-pixel row, radius 10,
+    many strip items per CTA: the case that exposed a load still in flight
+    when the buffer was refilled.  Repeated, since a race shows on some runs
+    only."""
+    rng = np.random.default_rng(24)
+    cases = [((777, 1999, 3), 3.22), ((777, 1999, 3), 3.9), ((500, 1999), 3.22), ((640, 1537, 4), 2.7)]
+    for shape, sigma in cases:
+        x = rng.random(shape, dtype=np.float32)
+        spec = [dict(op="gaussian", lo=(sigma,)), dict(op="fliplr")]
+        for _ in range(4):
+            check_spec(spec, [x])
