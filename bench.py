@@ -248,7 +248,8 @@ def ncu_traffic_per_px(workload, kind):
 
 
 KIND_NAMES = {0: "pointwise", 1: "gaussian tiles", 2: "rotate tiles", 3: "transpose",
-              4: "gaussian strip stream", 5: "rotate footprint", 8: "gaussian stream (mp_vh family)"}
+              4: "gaussian strip stream", 5: "rotate footprint", 8: "gaussian stream (mp_vh family)",
+              9: "gaussian + rotate fused (blur kept in shared memory)"}
 
 
 def time_graph(torch, graph, stream, steps, uuid):

@@ -330,7 +330,8 @@ MPStatus mpk_plan_destroy(MPPlan *plan);
 
 /* Launches launches [first, first+count) of a plan only, and describes
  * launch i (kind: 0 pointwise, 1 gaussian, 2 rotate, 3 transpose,
- * 4 streaming gaussian, 5 footprint-staged rotate; njobs
+ * 4 streaming gaussian, 5 footprint-staged rotate, 8 streaming gaussian
+ * (register-window family), 9 gaussian and rotate fused; njobs
  * images; tiles CTAs; bytes = algorithmic bytes moved: every input pixel read
  * once and every output pixel written once, float32). */
 MPStatus mpk_plan_launch_range(MPPlan *plan, int first, int count, void *stream);
@@ -363,6 +364,13 @@ MPStatus mpk_tune_set_stream(int cmid, int stages);
 /* Intermediate bytes one chunk of a fused batch may hold (at least 1 MB;
  * default 512 MB): a batch runs as one launch per segment per chunk. */
 MPStatus mpk_tune_set_chunk_bytes(size_t bytes);
+/* Fusion of a one-channel gaussian (radius <= 12; 1-channel source, or a
+ * 3-channel source whose prologue ends in rgb2grey) with the rotate after
+ * it into one kernel that keeps the blurred image in shared memory:
+ * 1 = on (default), 0 = off (two launches and an intermediate in HBM).
+ * Plans created afterwards follow the setting. */
+MPStatus mpk_tune_set_fuse(int enable);
+/* Clears the tuned tables and restores the defaults (fusion on). */
 void mpk_tune_clear(void);
 
 /* Differentiable chains on dense batches (the autograd path): B images of

@@ -27,9 +27,10 @@ BUILD = os.path.join(PKG, "_build")
 
 CU_SOURCES = ["mp_vh_c3.cu", "mp_vc_c3.cu", "mp_vh_c1.cu", "mp_vh_c4.cu", "mp_vc_c4.cu", "mp_vb_c3.cu", "mp_vb_c1.cu", "mp_vb_c4.cu", "mp_vd_c3.cu", "mp_vd_c1.cu", "mp_vd_c4.cu", "mp_stream_c3.cu", "mp_stream_grey3.cu",
               "mp_stream_c1.cu", "mp_runtime.cu", "mp_kernels.cu", "mp_stream.cu", "mp_rot.cu", "mp_vh.cu",
-              "mp_ops.cu", "mp_grad.cu", "mp_noalloc.cu", "mp_legacy.cu"]
+              "mp_ops.cu", "mp_grad.cu", "mp_noalloc.cu", "mp_legacy.cu", "mp_fuse.cu", "mp_fuse_c1.cu",
+              "mp_fuse_c3.cu"]
 C_SOURCES = ["py_module.c", "py_objects.c", "py_compose.c"]
-HEADERS = ["mp_internal.cuh", "mp_stream.cuh", "mp_vh.cuh", "py_common.h"]
+HEADERS = ["mp_internal.cuh", "mp_stream.cuh", "mp_vh.cuh", "mp_fuse.cuh", "py_common.h"]
 
 LIB_NAME = "libmillipyde_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

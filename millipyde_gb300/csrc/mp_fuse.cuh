@@ -49,14 +49,6 @@ using mp_vh::add2;
 using mp_vh::fma2;
 using mp_vh::ld4;
 
-// Per-launch shared-memory geometry (floats), sized on the host for the
-// largest job of the launch.
-struct FzGeom {
-    int stage;   // floats of one chunk stage (boxes x 128 x 16)
-    int gp;      // row pitch of G, V (per row of a pair: 2 gp) and B; = 4 (mod 16)
-    int offG;    // offset of G from the base
-};
-
 __device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
 
 // Footprint origin (pixels of the blurred image) of output tile lt: the
@@ -349,9 +341,9 @@ __device__ __forceinline__ float *fz_base(float4 *raw)
 
 // Persistent kernel: CTA b takes tiles b, b + grid, ... of the tile -> job map.
 #define MP_FZ_KERNEL(NAME, CIN)                                                                      \
-    __global__ void __launch_bounds__(mp_fz::NT, 1) NAME(const MPJob *__restrict__ jobs,             \
+    __global__ void __launch_bounds__(mp_fz::NT, 2) NAME(const MPJob *__restrict__ jobs,             \
                                                         const int *__restrict__ tile_job, int total, \
-                                                        const mp_fz::FzGeom g, int *err)             \
+                                                        const FzGeom g, int *err)             \
     {                                                                                               \
         extern __shared__ float4 mp_fz_dsmem4[];                                                    \
         float *base = mp_fz::fz_base(mp_fz_dsmem4);                                                 \

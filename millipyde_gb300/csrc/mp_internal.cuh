@@ -29,9 +29,11 @@
 // channel-preserving families), for radii up to MP_VH_RMAX.
 // RADJ / RDTH are the rotate adjoint's dx = R^T g and d theta passes on the
 // footprint-staged kernel (variant = 8 * mode + channels).
+// FUSE is a one-channel gaussian followed by a rotate in one kernel, the
+// blurred image kept in shared memory (mp_fuse.cuh).
 enum MPKind {
     MPK_POINT = 0, MPK_GAUSS = 1, MPK_ROTATE = 2, MPK_TRANSPOSE = 3, MPK_GSTREAM = 4, MPK_RSTREAM = 5,
-    MPK_RADJ = 6, MPK_RDTH = 7, MPK_VH = 8
+    MPK_RADJ = 6, MPK_RDTH = 7, MPK_VH = 8, MPK_FUSE = 9
 };
 #define MP_VH_RMAX 12
 #define MP_VH_RBIG 24   // largest bucket radius of the mp_vh.cuh kernels
@@ -144,7 +146,17 @@ struct MPJob {
     float cth, sth;            // ROTATE adjoint: cos/sin of the angle
     float wts_h[MP_MAX_TAPS];  // GAUSS: horizontal taps when hsep
     int vec_out;               // GSTREAM: destination rows 16-byte aligned (vector stores)
-    int bxw, byh;              // RSTREAM: footprint box (floats per row, rows)
+    int bxw, byh;              // RSTREAM: footprint box (floats per row, rows); FUSE: pixels
+    PwList epi2;               // FUSE: the gaussian's epilogue (applied before the rotate)
+};
+
+// Shared-memory geometry (floats) of a FUSE launch, sized for its largest
+// job: one chunk stage of the staged source region, the row pitch of the
+// blur planes (= 4 mod 16) and the offset of the plane G from the base.
+struct FzGeom {
+    int stage;
+    int gp;
+    int offG;
 };
 
 // ---------------------------------------------------------------------------
@@ -470,6 +482,18 @@ MPStatus mp_vh_prepare(int code, int *ctas_per_sm);
 MPStatus mp_vh_launch(int code, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
                       int *counter, cudaStream_t s);
 MPStatus mp_vh_launch_single(int code, const MPJob &job, int grid, int *err, cudaStream_t s);
+
+// Fused gaussian -> rotate (mp_fuse.cu): one output tile is 64 x 64 pixels
+// of the one-channel result.  mp_fz_geom sizes the shared memory for the
+// largest footprint box (pixels), radius and source channel count of a
+// launch; mp_fz_prepare raises the kernel's shared-memory limit and returns
+// the resident CTAs per SM (call outside capture).
+#define MP_FZ_RMAX 12
+bool mp_fz_supported(int cin, int radius);
+FzGeom mp_fz_geom(int box_max, int rmax, int cin, size_t *smem);
+MPStatus mp_fz_prepare(int cin, size_t smem, int *ctas_per_sm);
+MPStatus mp_fz_launch(int cin, const MPJob *jobs_dev, const int *tile_job, int total, const FzGeom &g, size_t smem,
+                      int grid, int *err, cudaStream_t s);
 
 // Streaming gaussian (mp_stream.cu).  mp_gs_prepare raises the
 // shared-memory limit and returns the resident CTAs per SM (call outside

@@ -44,7 +44,13 @@ struct Seg {
     double core_p[3];
     int cin, cmid, cout;
     int hin, win, hout, wout;
+    double rot_angle;   // FUSE: the rotate's angle (core_p holds the gaussian's sigma)
+    PwList epi2;        // FUSE: the gaussian's epilogue
 };
+
+// Fusion of a one-channel gaussian with the rotate after it (MPK_FUSE):
+// 1 = on (default), 0 = off (mpk_tune_set_fuse).
+static int mp_fuse_mode = 1;
 
 static bool mp_is_pointwise(int op)
 {
@@ -597,6 +603,8 @@ struct MPLaunch {
     int gauss[4];   // GAUSS: tile width, tile height, largest radius, all sources TMA-able
     GsGeom gs;      // GSTREAM: shared-memory geometry
     int grid;       // GSTREAM: persistent CTAs
+    FzGeom fz;      // FUSE: shared-memory geometry
+    int fz_cin;     // FUSE: source channels
 };
 
 struct MPPlanImpl {
@@ -614,7 +622,7 @@ struct MPPlanImpl {
 // Kernel variant of a segment (channel specialisation for GAUSS / ROTATE).
 static int mp_seg_variant(const Seg &sg)
 {
-    return (sg.kind == MPK_GAUSS || sg.kind == MPK_ROTATE) ? mp_variant(sg.cin, sg.cmid) : 0;
+    return (sg.kind == MPK_GAUSS || sg.kind == MPK_ROTATE || sg.kind == MPK_FUSE) ? mp_variant(sg.cin, sg.cmid) : 0;
 }
 
 static int mp_seg_key(const Seg &sg) { return sg.kind * 16 + mp_seg_variant(sg); }
@@ -657,7 +665,7 @@ struct MPTables {
         }
         if (L.njobs == 0) return MILLIPYDE_SUCCESS;
         if (kind < MPK_POINT_ADJ && kind != MPK_GSTREAM && kind != MPK_RSTREAM && kind != MPK_VH &&
-            kind != MPK_RADJ && kind != MPK_RDTH) {
+            kind != MPK_RADJ && kind != MPK_RDTH && kind != MPK_FUSE) {
             MPStatus e = mp_prepare_kind(kind, variant, smem);
             if (e != MILLIPYDE_SUCCESS) return e;
         }
@@ -917,6 +925,136 @@ static MPStatus mp_add_gauss_ordered(MPTables &T, std::vector<MPLaunch> &launche
     return T.add(launches, MPK_GAUSS, mp_variant(s0.cin, s0.cmid), smem, js, bytes);
 }
 
+// ---------------------------------------------------------------------------
+// Fused gaussian -> rotate (mp_fuse.cuh).
+// ---------------------------------------------------------------------------
+// Merges a one-channel gaussian segment and the rotate segment after it into
+// one FUSE segment when the fused kernel takes them: the blur keeps one
+// channel and has no mirror map, its radius is compiled there, the rotate
+// has no prologue, and the gaussian's source rows are TMA-legal (`in` is the
+// first segment's source; later sources are the plan's own intermediates,
+// always 16-byte aligned).
+static void mp_fuse_segments(std::vector<Seg> &segs, const MPImage &in)
+{
+    if (!mp_fuse_mode || !mp_get_encode_tiled()) return;
+    for (size_t k = 0; k + 1 < segs.size(); ++k) {
+        const Seg &g = segs[k], &r = segs[k + 1];
+        if (g.kind != MPK_GAUSS || r.kind != MPK_ROTATE) continue;
+        const int rad = (int)ceil(3.0 * g.core_p[0]);
+        if (g.cmid != 1 || g.cout != 1 || g.flip || !mp_fz_supported(g.cin, rad)) continue;
+        if (r.pro.n != 0 || r.cin != 1 || r.cmid != 1) continue;
+        if (k == 0 && ((in.pitch % 16) || ((uintptr_t)in.data % 16) || in.width <= 0 || in.height <= 0)) continue;
+        Seg f = g;
+        f.kind = MPK_FUSE;
+        f.epi2 = g.epi;
+        f.epi = r.epi;
+        f.flip = r.flip;
+        f.rot_angle = r.core_p[0];
+        f.cout = r.cout;
+        f.hout = r.hout;
+        f.wout = r.wout;
+        segs[k] = f;
+        segs.erase(segs.begin() + (long)k + 1);
+    }
+}
+
+// Footprint box (pixels) of a 64 x 64 output tile rotated by `angle`
+// degrees: the rotated tile's bounding box plus the bilinear neighbour and
+// the rounding margins of the rotate kernel (mp_fill_job_rot).
+static int mp_fz_box(double angle)
+{
+    const double th = angle * MP_DEG2RAD;
+    return (int)ceil(63.0 * fabs(cos(th)) + 63.0 * fabs(sin(th)) + 1e-6) + 4;
+}
+
+static MPStatus mp_fill_job_fuse(MPJob &J, const Seg &sg, const MPImage &in, const MPImage &out)
+{
+    memset(&J, 0, sizeof(J));
+    J.src = (const float *)in.data;
+    J.dst = (float *)out.data;
+    J.h = in.height;
+    J.w = in.width;
+    J.ho = out.height;
+    J.wo = out.width;
+    J.src_pitch = in.pitch / 4;
+    J.dst_pitch = out.pitch / 4;
+    J.cin = sg.cin;
+    J.cmid = 1;
+    J.cout = sg.cout;
+    J.flip = sg.flip;
+    J.pro = sg.pro;
+    J.epi = sg.epi;
+    J.epi2 = sg.epi2;
+    const double sigma = sg.core_p[0];
+    const int r = (int)ceil(3.0 * sigma);
+    if (r < 1 || r > MP_FZ_RMAX) return MP_ERROR_TOO_LARGE;
+    J.radius = r;
+    double e[MP_MAX_TAPS], sum = 0.0;
+    for (int k = -r; k <= r; ++k) {
+        e[k + r] = exp(-(double)(k * k) / (2.0 * sigma * sigma));
+        sum += e[k + r];
+    }
+    for (int k = 0; k < 2 * r + 1; ++k) J.wts[k] = (float)(e[k] / sum);
+    const double th_r = sg.rot_angle * MP_DEG2RAD;
+    const double scale = (double)(1LL << (MP_FIX_FRAC - 1));
+    J.cosq = llround(cos(th_r) * scale);
+    J.sinq = llround(sin(th_r) * scale);
+    J.tw = J.th = 64;
+    J.tiles_x = (out.width + 63) / 64;
+    J.ntiles = J.tiles_x * ((out.height + 63) / 64);
+    J.bxw = J.byh = mp_fz_box(sg.rot_angle);
+    mp_encode_tiled_fn enc = mp_get_encode_tiled();
+    if (!enc) return MP_ERROR_UNSUPPORTED_TYPE;
+    cuuint64_t gdim[2] = {(cuuint64_t)in.width * (cuuint64_t)sg.cin, (cuuint64_t)in.height};
+    cuuint64_t gstr[1] = {(cuuint64_t)in.pitch};
+    cuuint32_t box[2] = {128u, 16u};
+    cuuint32_t es[2] = {1u, 1u};
+    CUresult cr = enc(&J.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)in.data, gdim, gstr, box, es,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (cr != CUDA_SUCCESS) return MP_ERROR_UNSUPPORTED_TYPE;
+    J.use_tma = 1;
+    return MILLIPYDE_SUCCESS;
+}
+
+// One FUSE launch over images (sgs[i]: srcs[i] -> dsts[i]), jobs in radius
+// order (an SM's CTAs then run one compiled radius at a time).
+static MPStatus mp_add_fuse(MPTables &T, std::vector<MPLaunch> &launches, const std::vector<Seg> &sgs,
+                            const std::vector<MPImage> &srcs, const std::vector<MPImage> &dsts)
+{
+    if (sgs.empty()) return MILLIPYDE_SUCCESS;
+    std::vector<size_t> ord(sgs.size());
+    for (size_t i = 0; i < ord.size(); ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](size_t a, size_t b) { return sgs[a].core_p[0] < sgs[b].core_p[0]; });
+    std::vector<MPJob> js(sgs.size());
+    double bytes = 0.0;
+    int box_max = 0, rmax = 1;
+    for (size_t q = 0; q < ord.size(); ++q) {
+        const size_t i = ord[q];
+        MPStatus st = mp_fill_job_fuse(js[q], sgs[i], srcs[i], dsts[i]);
+        if (st != MILLIPYDE_SUCCESS) return st;
+        box_max = std::max(box_max, js[q].bxw);
+        rmax = std::max(rmax, js[q].radius);
+        bytes += 4.0 * ((double)srcs[i].height * srcs[i].width * srcs[i].channels +
+                        (double)dsts[i].height * dsts[i].width * dsts[i].channels);
+    }
+    const int cin = sgs[0].cin;
+    size_t smem = 0;
+    const FzGeom g = mp_fz_geom(box_max, rmax, cin, &smem);
+    int cps = 0;
+    MPStatus st = mp_fz_prepare(cin, smem, &cps);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    const size_t nl = launches.size();
+    st = T.add(launches, MPK_FUSE, mp_variant(cin, 1), smem, js, bytes);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    if (launches.size() > nl) {
+        launches.back().grid = cps * mp_num_sms();
+        launches.back().fz = g;
+        launches.back().fz_cin = cin;
+    }
+    return MILLIPYDE_SUCCESS;
+}
+
 // Job table upload plus the per-launch work counters of a plan.
 static MPStatus mp_plan_finish(MPPlanImpl *P, MPTables &T, cudaStream_t s)
 {
@@ -959,6 +1097,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             if (st != MILLIPYDE_SUCCESS) return st;
         }
         mp_segment(ops, in[i].channels, in[i].height, in[i].width, segs[i]);
+        mp_fuse_segments(segs[i], in[i]);
         const Seg &last = segs[i].back();
         if (!out[i].data && (long long)last.hout * last.wout > 0) return MP_ERROR_NULL_DATA;
         if (out[i].height != last.hout || out[i].width != last.wout ||
@@ -1033,6 +1172,19 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             int kind = segs[ch.imgs[0]][k].kind;
             int tw = 0, th = 0;
             size_t smem = 0;
+            if (kind == MPK_FUSE) {
+                std::vector<Seg> sgs;
+                std::vector<MPImage> srcs, dsts;
+                for (size_t q = 0; q < ch.imgs.size(); ++q) {
+                    const int img = ch.imgs[q];
+                    sgs.push_back(segs[img][k]);
+                    srcs.push_back((k == 0) ? in[img] : inter[q][k - 1]);
+                    dsts.push_back((k + 1 == nseg) ? out[img] : inter[q][k]);
+                }
+                st = mp_add_fuse(T, P->launches, sgs, srcs, dsts);
+                if (st != MILLIPYDE_SUCCESS) return st;
+                continue;
+            }
             if (kind == MPK_ROTATE) {
                 std::vector<Seg> sgs;
                 std::vector<MPImage> srcs, dsts;
@@ -1095,6 +1247,9 @@ static MPStatus mp_plan_launch_one(const MPPlanImpl *P, size_t idx, cudaStream_t
         return mp_vh_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles, L.grid,
                             P->err, P->counters + idx, s);
     }
+    if (L.kind == MPK_FUSE)
+        return mp_fz_launch(L.fz_cin, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles, L.fz, L.smem,
+                            L.grid, P->err, s);
     if (L.kind == MPK_RSTREAM || L.kind == MPK_RADJ || L.kind == MPK_RDTH)
         return mp_ro_launch(L.variant, P->jobs_dev + L.job_off, P->tiles_dev + L.tile_off, L.total_tiles,
                             L.gauss[0], L.grid, P->err, s);
@@ -2326,8 +2481,16 @@ extern "C" MPStatus mpk_tune_set_chunk_bytes(size_t bytes)
     return MILLIPYDE_SUCCESS;
 }
 
+extern "C" MPStatus mpk_tune_set_fuse(int enable)
+{
+    if (enable != 0 && enable != 1) return MP_ERROR_INVALID_ARGS;
+    mp_fuse_mode = enable;
+    return MILLIPYDE_SUCCESS;
+}
+
 extern "C" void mpk_tune_clear(void)
 {
+    mp_fuse_mode = 1;
     std::lock_guard<std::mutex> lk(mp_tune_mutex);
     mp_tune_table.clear();
     mp_stream_tune.clear();
