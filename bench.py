@@ -700,6 +700,8 @@ def run_ours(args):
     L = _abi.lib()
     torch.cuda.set_device(0)
     uuid = gpu_uuid(torch)
+    if args.fuse != "auto":
+        _abi.check(L.mpk_tune_set_fuse(1 if args.fuse == "on" else 0))
 
     if args.workload in ("grad4", "grad5"):
         print(json.dumps(bench_grad(args, torch, L, uuid, args.workload)), flush=True)
@@ -755,6 +757,8 @@ def main():
                     help="ragged batch size (default 1000; profiling runs use a smaller batch)")
     ap.add_argument("--legs", default="all", choices=["all", "fused"],
                     help="'fused' times only the fused plan (profiling runs)")
+    ap.add_argument("--fuse", default="auto", choices=["auto", "on", "off"],
+                    help="gaussian + rotate fusion: the tuned/default choice, or forced (comparison runs)")
     ap.add_argument("--workload", default="ragged", choices=["ragged", "uniform", "grad4", "grad5"],
                     help="ragged: the headline line with every other configuration as extra keys; "
                          "the others print one configuration alone")

@@ -364,13 +364,24 @@ MPStatus mpk_tune_set_stream(int cmid, int stages);
 /* Intermediate bytes one chunk of a fused batch may hold (at least 1 MB;
  * default 512 MB): a batch runs as one launch per segment per chunk. */
 MPStatus mpk_tune_set_chunk_bytes(size_t bytes);
+/* Geometry of the persistent kernels, per launch kind (5 footprint rotate,
+ * 8 streaming gaussian, 9 fused gaussian + rotate); value 0 restores the
+ * built-in choice.  param 0: work items per resident CTA of a streaming
+ * gaussian launch (rows per item follow; kind 8 only, 1..64); param 1: cap
+ * on resident CTAs per SM (1..32); param 2: cap on the streaming gaussian's
+ * strip width in columns (kind 8 only, a multiple of 8 from 64).  Set by
+ * millipyde_gb300/autotune.py from timings; plans created afterwards follow
+ * it. */
+MPStatus mpk_tune_set_kernel(int kind, int param, int value);
+MPStatus mpk_tune_get_kernel(int kind, int param, int *value);
 /* Fusion of a one-channel gaussian (radius <= 12; 1-channel source, or a
  * 3-channel source whose prologue ends in rgb2grey) with the rotate after
  * it into one kernel that keeps the blurred image in shared memory:
- * 1 = on (default), 0 = off (two launches and an intermediate in HBM).
- * Plans created afterwards follow the setting. */
+ * 1 = on, 0 = off (the default: two launches and an intermediate in HBM).
+ * The autotuner times both and records the faster.  Plans created
+ * afterwards follow the setting. */
 MPStatus mpk_tune_set_fuse(int enable);
-/* Clears the tuned tables and restores the defaults (fusion on). */
+/* Clears the tuned tables and restores the defaults (fusion off). */
 void mpk_tune_clear(void);
 
 /* Differentiable chains on dense batches (the autograd path): B images of

@@ -1,4 +1,5 @@
-"""Autotuner for the gaussian kernel's tile shape.
+"""Autotuner: the gaussian tile kernel's tile shape, the persistent
+kernels' geometry and the gaussian -> rotate fusion split.
 
 The gaussian segment kernel processes tw x th output pixels per CTA; the best
 shape depends on the channel variant (source channels, channels after the
@@ -7,6 +8,13 @@ memory and CTAs per SM).  tune_gaussian() times every candidate tile on the
 device -- a plan over a batch of synthetic images, CUDA events around its
 launch -- and records the fastest with mpk_tune_set_gauss_tile; the planner
 then uses it for every batch and per-op call in that radius range.
+
+tune_kernels() does the same for the hot kernels' launch geometry
+(mpk_tune_set_kernel: work items per CTA, CTAs per SM and strip width of the
+streaming gaussian, CTAs per SM of the footprint rotate and of the fused
+gaussian + rotate) on a ragged and a uniform synthetic batch, coordinate by
+coordinate, and decides the fusion split (mpk_tune_set_fuse) by timing the
+uniform chain fused and split.
 
 Results persist in a JSON table keyed by GPU name: the package ships one for
 GB300 (tune_gb300.json, produced by tune_defaults() on a GB300), applied at
@@ -103,16 +111,139 @@ DEFAULT_CASES = [
 ]
 
 
-def tune_defaults(path=None, cases=DEFAULT_CASES, **kw):
-    """Tunes the common cases and writes the JSON table."""
+def tune_defaults(path=None, cases=DEFAULT_CASES, kernels=True, **kw):
+    """Tunes the common cases (gaussian tiles, then the kernel geometry and
+    the fusion split) and writes the JSON table."""
     entries = []
     for cin, cmid, pro, r, rr in cases:
         res = tune_gaussian(cin, cmid, pro, r, radius_range=rr, apply=False, **kw)
         if res:
             entries.append(res)
+    if kernels:
+        entries += tune_kernels()
     save(entries, path)
     load(path)
     return entries
+
+
+# Launch kinds of mpk_plan_launch_info and mpk_tune_set_kernel.
+KIND_ROTATE, KIND_GAUSS_STREAM, KIND_FUSED = 5, 8, 9
+PARAM_ITEMS, PARAM_CTAS, PARAM_STRIP = 0, 1, 2
+# (kind, param, candidate values; 0 = the built-in choice)
+KERNEL_CANDIDATES = [
+    (KIND_GAUSS_STREAM, PARAM_ITEMS, [0, 2, 8, 16]),
+    (KIND_GAUSS_STREAM, PARAM_CTAS, [0, 2]),
+    (KIND_GAUSS_STREAM, PARAM_STRIP, [0, 128]),
+    (KIND_ROTATE, PARAM_CTAS, [0, 2, 3]),
+    (KIND_FUSED, PARAM_CTAS, [0, 1]),
+]
+
+
+class _Batch:
+    """A synthetic batch and its chain on the device, timed as one plan."""
+
+    def __init__(self, kind, n):
+        import math
+
+        import numpy as np
+        import torch
+
+        rng = np.random.default_rng(7)
+        if kind == "ragged":
+            lo, hi = math.log(64), math.log(2048)
+            sizes = [(int(round(math.exp(rng.uniform(lo, hi)))), int(round(math.exp(rng.uniform(lo, hi)))))
+                     for _ in range(n)]
+            self.stages = _abi.stages(
+                _abi.stage("rotate", random=True, lo=(-45,), hi=(45,)),
+                _abi.stage("gaussian", random=True, lo=(0.5,), hi=(4.0,)),
+                _abi.stage("adjust_gamma", random=True, lo=(0.5, 1.0), hi=(2.0, 1.0)),
+                _abi.stage("brightness", random=True, lo=(-0.2,), hi=(0.2,)),
+                _abi.stage("fliplr", probability=0.5))
+            self.nst, cout = 5, 3
+        else:
+            sizes = [(1024, 1024)] * n
+            self.stages = _abi.stages(_abi.stage("rgb2grey"), _abi.stage("gaussian", 3.0),
+                                      _abi.stage("rotate", 17.0), _abi.stage("adjust_gamma", 0.8, 1.0))
+            self.nst, cout = 4, 1
+        self.keep, ins, outs = [], [], []
+        for h, w in sizes:
+            pi, po = (w * 12 + 15) // 16 * 16, (w * cout * 4 + 15) // 16 * 16
+            x = torch.rand((h, pi // 4), device="cuda")
+            y = torch.empty((h, po // 4), device="cuda")
+            self.keep += [x, y]
+            ins.append(_abi.image(x.data_ptr(), h, w, 3, pi))
+            outs.append(_abi.image(y.data_ptr(), h, w, cout, po))
+        self.ins, self.outs, self.n = _abi.images(ins), _abi.images(outs), n
+
+    def time(self, reps=5):
+        """Milliseconds per pass of the plan (CUDA events), or None."""
+        import torch
+
+        L = _abi.lib()
+        sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        plan = C.c_void_p()
+        if L.mpk_plan_create(self.stages, self.nst, self.ins, self.outs, self.n, 1, 0, sp, C.byref(plan)) != 0:
+            return None
+        try:
+            _abi.check(L.mpk_plan_launch(plan, sp))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                _abi.check(L.mpk_plan_launch(plan, sp))
+            e1.record()
+            e1.synchronize()
+            return e0.elapsed_time(e1) / reps
+        finally:
+            L.mpk_plan_destroy(plan)
+            torch.cuda.synchronize()
+
+
+def tune_kernels(ragged_images=150, uniform_images=24, candidates=KERNEL_CANDIDATES, apply=True):
+    """Coordinate search over the kernel geometry knobs (each timed on the
+    batch whose launches it affects) and the fusion split; returns the
+    entries (recorded with mpk_tune_set_kernel / mpk_tune_set_fuse when
+    apply)."""
+    L = _abi.lib()
+    batches = {"ragged": _Batch("ragged", ragged_images), "uniform": _Batch("uniform", uniform_images)}
+    entries = []
+    # fusion split on the uniform chain
+    times = {}
+    for mode, name in ((1, "fused"), (0, "split")):
+        _abi.check(L.mpk_tune_set_fuse(mode))
+        times[name] = batches["uniform"].time()
+    fuse = 1 if (times["fused"] or 1e30) <= (times["split"] or 1e30) else 0
+    _abi.check(L.mpk_tune_set_fuse(fuse))
+    entries.append({"fuse": fuse, "ms": {k: round(v, 5) for k, v in times.items() if v}})
+    for kind, param, values in candidates:
+        batch = batches["uniform" if kind == KIND_FUSED else "ragged"]
+        times = {}
+        for v in values:
+            if L.mpk_tune_set_kernel(kind, param, v) != 0:
+                continue
+            t = batch.time()
+            if t is not None:
+                times[v] = t
+        best = min(times, key=times.get) if times else 0
+        _abi.check(L.mpk_tune_set_kernel(kind, param, best))
+        entries.append({"kernel_kind": kind, "param": param, "value": best,
+                        "ms": {str(k): round(t, 5) for k, t in times.items()}})
+    if not apply:
+        _apply(entries, clear=False, undo=True)
+    return entries
+
+
+def _apply(entries, clear=False, undo=False):
+    L = _abi.lib()
+    n = 0
+    for e in entries:
+        if "fuse" in e:
+            n += L.mpk_tune_set_fuse(0 if undo else e["fuse"]) == 0
+        elif "kernel_kind" in e:
+            n += L.mpk_tune_set_kernel(e["kernel_kind"], e["param"], 0 if undo else e["value"]) == 0
+        elif not undo and L.mpk_tune_set_gauss_tile(e["cin"], e["cmid"], e["has_pro"], e["radius_lo"],
+                                                    e["radius_hi"], e["tile"][0], e["tile"][1]) == 0:
+            n += 1
+    return n
 
 
 def _device_name():
@@ -147,11 +278,4 @@ def load(path=None):
             data = json.load(f)
     except (OSError, ValueError):
         return 0
-    L = _abi.lib()
-    name = _device_name()
-    n = 0
-    for e in data.get(name, []):
-        if L.mpk_tune_set_gauss_tile(e["cin"], e["cmid"], e["has_pro"], e["radius_lo"], e["radius_hi"],
-                                     e["tile"][0], e["tile"][1]) == 0:
-            n += 1
-    return n
+    return _apply(data.get(_device_name(), []))

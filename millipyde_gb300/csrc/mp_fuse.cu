@@ -30,7 +30,7 @@ FzGeom mp_fz_geom(int box_max, int rmax, int cin, size_t *smem)
     const int sw = box_max + 2 * rmax;                  // widest source region (pixels)
     g.gp = ((sw + 8 + 15) & ~15) + 4;                   // = 4 (mod 16): conflict-free row-pair loads
     const int nb = (3 + sw * cin + 127) / 128;          // boxes of 128 floats per chunk row
-    g.stage = nb * 128 * 16;
+    g.stage = nb * 128 * MP_FZ_CR;
     int area = 2 * g.stage;
     if (area < 96 * g.gp) area = 96 * g.gp;
     g.offG = 32 + ((area + 31) & ~31);

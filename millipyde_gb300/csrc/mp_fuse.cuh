@@ -39,7 +39,7 @@ namespace mp_fz {
 constexpr int NT = 256;    // threads per CTA
 constexpr int TW = 64;     // output tile (one channel)
 constexpr int TH = 64;
-constexpr int CR = 16;     // source rows per staged chunk
+constexpr int CR = MP_FZ_CR; // source rows per staged chunk
 constexpr int BXF = 128;   // floats per TMA box row
 constexpr int VG = 24;     // vertical-pass output rows per thread group
 constexpr int NVG = 4;     // thread groups: 4 x 24 rows >= the tallest footprint

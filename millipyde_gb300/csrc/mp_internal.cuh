@@ -478,6 +478,8 @@ int mp_vh_bucket(int radius);
 int mp_vh_dot_code(int c, int radius);
 int mp_vh_strip(int radius, int cm);
 int mp_vh_fit_strip(int radius, int w, int cm);
+// Tuned cap on strip widths (columns, a multiple of 8 from 64; 0: none).
+void mp_vh_set_strip_cap(int cols);
 MPStatus mp_vh_prepare(int code, int *ctas_per_sm);
 MPStatus mp_vh_launch(int code, const MPJob *jobs_dev, const int *tile_job, int total, int grid, int *err,
                       int *counter, cudaStream_t s);
@@ -489,6 +491,7 @@ MPStatus mp_vh_launch_single(int code, const MPJob &job, int grid, int *err, cud
 // launch; mp_fz_prepare raises the kernel's shared-memory limit and returns
 // the resident CTAs per SM (call outside capture).
 #define MP_FZ_RMAX 12
+#define MP_FZ_CR 16    // source rows per TMA chunk (the tensor map's box height)
 bool mp_fz_supported(int cin, int radius);
 FzGeom mp_fz_geom(int box_max, int rmax, int cin, size_t *smem);
 MPStatus mp_fz_prepare(int cin, size_t smem, int *ctas_per_sm);

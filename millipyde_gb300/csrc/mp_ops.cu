@@ -49,8 +49,30 @@ struct Seg {
 };
 
 // Fusion of a one-channel gaussian with the rotate after it (MPK_FUSE):
-// 1 = on (default), 0 = off (mpk_tune_set_fuse).
-static int mp_fuse_mode = 1;
+// 1 = on, 0 = off (default; mpk_tune_set_fuse, chosen by the autotuner from
+// timings of both).
+static int mp_fuse_mode = 0;
+
+// Tuned geometry of the persistent kernels per launch kind (5 footprint
+// rotate, 8 streaming gaussian, 9 fused gaussian + rotate), set by the
+// autotuner through mpk_tune_set_kernel; 0 keeps the built-in choice.
+enum { MP_TK_ITEMS = 0, MP_TK_CTAS = 1, MP_TK_STRIP = 2, MP_TK_NPARAM = 3 };
+static int mp_ktune[16][MP_TK_NPARAM];
+static std::mutex mp_ktune_mutex;
+
+static int mp_tuned(int kind, int param)
+{
+    std::lock_guard<std::mutex> lk(mp_ktune_mutex);
+    return mp_ktune[kind & 15][param];
+}
+
+// Resident CTAs per SM a persistent launch of `kind` uses: the occupancy
+// limit, or the tuned cap when it is lower.
+static int mp_cap_ctas(int kind, int cps)
+{
+    const int m = mp_tuned(kind, MP_TK_CTAS);
+    return (m > 0 && m < cps) ? m : cps;
+}
 
 static bool mp_is_pointwise(int op)
 {
@@ -520,7 +542,7 @@ static bool mp_rot_setup(int c, int buf_floats, int *grid)
         cudaGetLastError();
         return false;
     }
-    *grid = cps * mp_num_sms();
+    *grid = mp_cap_ctas(MPK_RSTREAM, cps) * mp_num_sms();
     return true;
 }
 
@@ -736,7 +758,8 @@ static MPStatus mp_fill_job_vh(MPJob &J, const Seg &sg, const MPImage &in, const
 // at least 32 rows (the 2R head rows of an item are loads only).
 static int mp_vh_rows(long long strip_rows, int grid)
 {
-    const long long target = 4LL * (grid > 0 ? grid : 1);
+    const int items = mp_tuned(MPK_VH, MP_TK_ITEMS);
+    const long long target = (long long)(items > 0 ? items : 4) * (grid > 0 ? grid : 1);
     long long rs = (strip_rows + target - 1) / target;
     if (rs < 32) rs = 32;
     if (rs > 4096) rs = 4096;
@@ -755,7 +778,7 @@ static MPStatus mp_vh_run_single(const Seg &sg, const MPImage &in, const MPImage
         cudaGetLastError();
         return MILLIPYDE_SUCCESS;
     }
-    const int grid = cps * mp_num_sms();
+    const int grid = mp_cap_ctas(MPK_VH, cps) * mp_num_sms();
     const int sw = mp_vh_fit_strip(mp_vh_bucket(r), in.width, cm);
     MPJob J;
     MPStatus st = mp_fill_job_vh(J, sg, in, out,
@@ -860,7 +883,7 @@ static MPStatus mp_add_gauss_ordered(MPTables &T, std::vector<MPLaunch> &launche
         int cps = 0;
         if (mp_vh_prepare(code[a], &cps) != MILLIPYDE_SUCCESS) vh = false;
         runs.push_back({a, b});
-        grids.push_back(cps * mp_num_sms());
+        grids.push_back(mp_cap_ctas(MPK_VH, cps) * mp_num_sms());
         a = b;
     }
     if (vh) {
@@ -1007,7 +1030,7 @@ static MPStatus mp_fill_job_fuse(MPJob &J, const Seg &sg, const MPImage &in, con
     if (!enc) return MP_ERROR_UNSUPPORTED_TYPE;
     cuuint64_t gdim[2] = {(cuuint64_t)in.width * (cuuint64_t)sg.cin, (cuuint64_t)in.height};
     cuuint64_t gstr[1] = {(cuuint64_t)in.pitch};
-    cuuint32_t box[2] = {128u, 16u};
+    cuuint32_t box[2] = {128u, (cuuint32_t)MP_FZ_CR};
     cuuint32_t es[2] = {1u, 1u};
     CUresult cr = enc(&J.tmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)in.data, gdim, gstr, box, es,
                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -1048,7 +1071,7 @@ static MPStatus mp_add_fuse(MPTables &T, std::vector<MPLaunch> &launches, const 
     st = T.add(launches, MPK_FUSE, mp_variant(cin, 1), smem, js, bytes);
     if (st != MILLIPYDE_SUCCESS) return st;
     if (launches.size() > nl) {
-        launches.back().grid = cps * mp_num_sms();
+        launches.back().grid = mp_cap_ctas(MPK_FUSE, cps) * mp_num_sms();
         launches.back().fz = g;
         launches.back().fz_cin = cin;
     }
@@ -2481,6 +2504,29 @@ extern "C" MPStatus mpk_tune_set_chunk_bytes(size_t bytes)
     return MILLIPYDE_SUCCESS;
 }
 
+extern "C" MPStatus mpk_tune_set_kernel(int kind, int param, int value)
+{
+    if ((kind != MPK_RSTREAM && kind != MPK_VH && kind != MPK_FUSE) || param < 0 || param >= MP_TK_NPARAM ||
+        value < 0)
+        return MP_ERROR_INVALID_ARGS;
+    if (param == MP_TK_ITEMS && (kind != MPK_VH || value > 64)) return MP_ERROR_INVALID_ARGS;
+    if (param == MP_TK_CTAS && value > 32) return MP_ERROR_INVALID_ARGS;
+    if (param == MP_TK_STRIP) {
+        if (kind != MPK_VH || (value && (value < 64 || value % 8))) return MP_ERROR_INVALID_ARGS;
+        mp_vh_set_strip_cap(value);
+    }
+    std::lock_guard<std::mutex> lk(mp_ktune_mutex);
+    mp_ktune[kind][param] = value;
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_tune_get_kernel(int kind, int param, int *value)
+{
+    if (kind < 0 || kind > 15 || param < 0 || param >= MP_TK_NPARAM || !value) return MP_ERROR_INVALID_ARGS;
+    *value = mp_tuned(kind, param);
+    return MILLIPYDE_SUCCESS;
+}
+
 extern "C" MPStatus mpk_tune_set_fuse(int enable)
 {
     if (enable != 0 && enable != 1) return MP_ERROR_INVALID_ARGS;
@@ -2490,7 +2536,12 @@ extern "C" MPStatus mpk_tune_set_fuse(int enable)
 
 extern "C" void mpk_tune_clear(void)
 {
-    mp_fuse_mode = 1;
+    {
+        std::lock_guard<std::mutex> lk(mp_ktune_mutex);
+        memset(mp_ktune, 0, sizeof(mp_ktune));
+    }
+    mp_vh_set_strip_cap(0);
+    mp_fuse_mode = 0;
     std::lock_guard<std::mutex> lk(mp_tune_mutex);
     mp_tune_table.clear();
     mp_stream_tune.clear();

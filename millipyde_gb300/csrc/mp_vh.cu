@@ -76,9 +76,15 @@ int mp_vh_strip(int radius, int cm)
 // Strip width in columns for an image of width w pixels (w * cm columns):
 // the fewest strips of at most mp_vh_strip(radius, cm) columns, evened out
 // and rounded up to 8.
+// Tuned cap on the strip width in columns (0: the kernel's limit).
+static int mp_vh_strip_cap = 0;
+
+void mp_vh_set_strip_cap(int cols) { mp_vh_strip_cap = cols; }
+
 int mp_vh_fit_strip(int radius, int w, int cm)
 {
-    const int maxw = mp_vh_strip(radius, cm);
+    int maxw = mp_vh_strip(radius, cm);
+    if (mp_vh_strip_cap >= 64 && mp_vh_strip_cap < maxw) maxw = mp_vh_strip_cap;
     const int wc = w * cm;
     const int n = (wc + maxw - 1) / maxw;
     const int sw = ((wc + n - 1) / n + 7) & ~7;

@@ -123,56 +123,15 @@ __device__ __forceinline__ int chan_of(int f)
     return c < 0 ? c + CM : c;
 }
 
-// Mirrored store (fliplr) of floats xo0 .. xo0 + 7 of an interleaved
-// CM-channel row: fliplr moves pixels and keeps their channel order, so
-// float f = xo0 + k goes to (wo - 1 - f / CM) * CM + f % CM = B - k + 2 c
-// with B = (wo - 1) * CM - xo0 and c = (C0 + k) % CM, C0 = xo0 % CM: for a
-// given C0 every offset is a compile-time constant.  Floats from W on are
-// not stored.
-template <int CM, int C0>
-__device__ __forceinline__ void st_mirror8(float *b, int nvalid, const float (&o)[8])
-{
-    if (nvalid >= 8) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) b[-k + 2 * ((C0 + k) % CM)] = o[k];
-    } else {
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (k < nvalid) b[-k + 2 * ((C0 + k) % CM)] = o[k];
-    }
-}
-
-template <int CM>
-__device__ __forceinline__ void store8(float *drow, int xo0, int W, int wo, bool flip, const float (&o)[8])
-{
-    const int nvalid = W - xo0;
-    if (!flip) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-            if (k < nvalid) drow[xo0 + k] = o[k];
-        return;
-    }
-    float *b = drow + (wo - 1) * CM - xo0;
-    if constexpr (CM == 1) {
-        st_mirror8<1, 0>(b, nvalid, o);
-    } else {
-        const int c0 = xo0 % CM;
-        if (c0 == 0) st_mirror8<CM, 0>(b, nvalid, o);
-        else if (c0 == 1) st_mirror8<CM, 1>(b, nvalid, o);
-        else if (c0 == 2) st_mirror8<CM, 2>(b, nvalid, o);
-        else st_mirror8<CM, 3>(b, nvalid, o);
-    }
-}
-
 // One strip item with compiled radius R.  The strip is J.tw output columns
 // wide (a multiple of 8, at most 2*NT - 2*R4); window rows are counted from
 // source row y0 - R8 (R8 = R rounded up to 4) so that every step of VR rows
 // is exactly one staged group.
-// Every kernel keeps the symmetric taps once (R + 1 tap registers): the
-// vertical pass adds the two window rows of each tap pair before
-// multiplying.  Radii above MP_VH_RMAX are buckets: a job of radius r <= R
-// runs with its taps centred in 2R + 1 (zeros outside) and the horizontal
-// pass consumes the tile row in order.
+// Radii above MP_VH_RMAX are buckets: a job of radius r <= R runs with its
+// taps centred in 2R + 1 (zeros outside), the vertical pass adds the two
+// window rows of each symmetric tap pair before multiplying (R + 1 tap
+// registers instead of 2R + 1) and the horizontal pass consumes the tile row
+// in order.
 // DOT: the d sigma mode of the gaussian's adjoint.  The horizontal pass
 // uses J.wts_h (the vertical pass J.wts), nothing is stored, and the sum of
 // output * J.aux (the output-space gradient) over the item is added to
@@ -183,10 +142,10 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     constexpr bool BIG = R > MP_VH_RMAX;
     constexpr int VR = MP_VH_VR, VW = 2 * NT + 4, NW = NT / 32;
     constexpr int NTAP = 2 * R + 1, RC = R * CM, R4 = (RC + 3) & ~3, E = R4 - RC;
-    constexpr int NW2 = R + 1;                            // tap registers: the taps are symmetric
-    // the exact-radius kernels (every family) compute two output rows per
+    constexpr int NW2 = BIG ? R + 1 : NTAP;               // tap registers
+    // the plain one-channel family computes two output rows per
     // horizontal work item as packed pairs
-    constexpr bool PAIR = !BIG && !DOT;
+    constexpr bool PAIR = CM == 1 && !BIG && !DOT;
     constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
     constexpr int D = R8 - R;                             // tap offset inside the window
     constexpr int NWIN = VR + 2 * R8;
@@ -307,8 +266,8 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     float2 w2[NW2];
 #pragma unroll
     for (int m = 0; m < NW2; ++m) w2[m] = make_float2(taps[m], taps[m]);
-    // tap m of 2R + 1 (symmetric storage: w[m] = w[2R - m])
-    auto tap = [&](int m) -> float { return w2[m <= R ? m : 2 * R - m].x; };
+    // tap m of 2R + 1 (symmetric storage for the buckets)
+    auto tap = [&](int m) -> float { return BIG ? w2[m <= R ? m : 2 * R - m].x : w2[m].x; };
     float hw[DOT ? NTAP : 1];
     if constexpr (DOT) {
 #pragma unroll
@@ -356,12 +315,15 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
             float2 prev = make_float2(0.f, 0.f);
 #pragma unroll
             for (int o = 0; o < VR; ++o) {
-                // symmetric taps: the two window rows of each pair are added
-                // first (R + 1 tap registers, the same instruction count)
                 float2 a = make_float2(0.f, 0.f);
-                a = fma2(w2[R], win[o + D + R], a);
+                if constexpr (BIG) {
+                    a = fma2(w2[R], win[o + D + R], a);
 #pragma unroll
-                for (int k = 0; k < R; ++k) a = fma2(w2[k], add2(win[o + D + k], win[o + D + 2 * R - k]), a);
+                    for (int k = 0; k < R; ++k) a = fma2(w2[k], add2(win[o + D + k], win[o + D + 2 * R - k]), a);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < NTAP; ++k) a = fma2(w2[k], win[o + D + k], a);
+                }
                 if constexpr (PAIR) {
                     if (o & 1)
                         *reinterpret_cast<float4 *>(tb + (o >> 1) * (2 * VW)) = make_float4(prev.x, a.x, prev.y, a.y);
@@ -406,7 +368,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                                     o2[k].y = fmaf(hw[t / CM], pc[u].y, o2[k].y);
                                 } else {
                                     const int m = t / CM;
-                                    o2[k] = fma2(w2[m <= R ? m : 2 * R - m], pc[u], o2[k]);
+                                    o2[k] = fma2(w2[BIG ? (m <= R ? m : 2 * R - m) : m], pc[u], o2[k]);
                                 }
                             }
                         }
@@ -449,13 +411,25 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                     if (vec && xo0 + 8 <= W) {
                         *reinterpret_cast<float4 *>(drow + xo0) = make_float4(o[0], o[1], o[2], o[3]);
                         *reinterpret_cast<float4 *>(drow + xo0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                    } else if constexpr (CM == 1) {
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            if (xo0 + k < W) drow[flip ? wo - 1 - (xo0 + k) : xo0 + k] = o[k];
                     } else if (CM == 4 && flip && J.vec_out && xo0 + 8 <= W) {
                         // two whole pixels, mirrored: one float4 each
                         const int px = xo0 >> 2;
                         *reinterpret_cast<float4 *>(drow + (wo - 1 - px) * 4) = make_float4(o[0], o[1], o[2], o[3]);
                         *reinterpret_cast<float4 *>(drow + (wo - 2 - px) * 4) = make_float4(o[4], o[5], o[6], o[7]);
                     } else {
-                        store8<CM>(drow, xo0, W, wo, flip, o);
+                        // fliplr mirrors pixels and keeps the channel order
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            const int f = xo0 + k;
+                            if (f < W) {
+                                const int px = f / CM, c = f - px * CM;
+                                drow[flip ? (wo - 1 - px) * CM + c : f] = o[k];
+                            }
+                        }
                     }
                 };
                 float oa[8], ob[8];
@@ -552,13 +526,25 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                 if (vec && xo0 + 8 <= W) {
                     *reinterpret_cast<float4 *>(drow + xo0) = make_float4(o[0], o[1], o[2], o[3]);
                     *reinterpret_cast<float4 *>(drow + xo0 + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                } else if constexpr (CM == 1) {
+#pragma unroll
+                    for (int k = 0; k < 8; ++k)
+                        if (xo0 + k < W) drow[flip ? wo - 1 - (xo0 + k) : xo0 + k] = o[k];
                 } else if (CM == 4 && flip && J.vec_out && xo0 + 8 <= W) {
                     // two whole pixels, mirrored: one float4 each
                     const int px = xo0 >> 2;
                     *reinterpret_cast<float4 *>(drow + (wo - 1 - px) * 4) = make_float4(o[0], o[1], o[2], o[3]);
                     *reinterpret_cast<float4 *>(drow + (wo - 2 - px) * 4) = make_float4(o[4], o[5], o[6], o[7]);
                 } else {
-                    store8<CM>(drow, xo0, W, wo, flip, o);
+                    // fliplr mirrors pixels and keeps the channel order
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const int f = xo0 + k;
+                        if (f < W) {
+                            const int px = f / CM, c = f - px * CM;
+                            drow[flip ? (wo - 1 - px) * CM + c : f] = o[k];
+                        }
+                    }
                 }
             }
         }
