@@ -25,7 +25,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 
-CU_SOURCES = ["mp_vh_c3.cu", "mp_vc_c3.cu", "mp_vh_c1.cu", "mp_vh_c4.cu", "mp_vc_c4.cu", "mp_vb_c3.cu", "mp_vb_c1.cu", "mp_vb_c4.cu", "mp_vd_c3.cu", "mp_vd_c1.cu", "mp_vd_c4.cu", "mp_stream_c3.cu", "mp_stream_grey3.cu",
+CU_SOURCES = ["mp_vh_c3.cu", "mp_vc_c3.cu", "mp_vc_c3_lo.cu", "mp_vc_c3_mid.cu", "mp_vh_c1.cu", "mp_vh_c4.cu", "mp_vc_c4.cu", "mp_vb_c3.cu", "mp_vb_c1.cu", "mp_vb_c4.cu", "mp_vd_c3.cu", "mp_vd_c1.cu", "mp_vd_c4.cu", "mp_stream_c3.cu", "mp_stream_grey3.cu",
               "mp_stream_c1.cu", "mp_runtime.cu", "mp_kernels.cu", "mp_stream.cu", "mp_rot.cu", "mp_vh.cu",
               "mp_ops.cu", "mp_grad.cu", "mp_noalloc.cu", "mp_legacy.cu", "mp_fuse.cu", "mp_fuse_c1.cu",
               "mp_fuse_c3.cu"]

@@ -467,7 +467,9 @@ size_t mp_ro_smem(int buf_floats);
 // single-channel family (cmid 1), 4 + C (7, 8) for the channel-preserving
 // family on C = 3 or 4 interleaved channels, plus 16 for the radius buckets
 // above MP_VH_RMAX (1-channel sources, RGB and RGBA only), plus 32 for the
-// dot mode of the gaussian's adjoint (mp_vd*.cu); -1 if no kernel
+// dot mode of the gaussian's adjoint (mp_vd*.cu), plus 64 / 128 for the RGB
+// channel-preserving kernels of radii 1..4 / 5..8 (mp_vc_c3_lo.cu,
+// mp_vc_c3_mid.cu: own register budgets, 4 CTAs per SM); -1 if no kernel
 // takes (cin, cmid, radius).  mp_vh_bucket is the radius a job runs with
 // (its strip halo).  Strips are counted in columns: pixels when cm = 1,
 // floats of the interleaved row otherwise.

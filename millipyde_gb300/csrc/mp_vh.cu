@@ -15,6 +15,8 @@ MP_VH_DECL(mp_vh_c1)
 MP_VH_DECL(mp_vh_c3)
 MP_VH_DECL(mp_vh_c4)
 MP_VH_DECL(mp_vc_c3)
+MP_VH_DECL(mp_vc_c3_lo)
+MP_VH_DECL(mp_vc_c3_mid)
 MP_VH_DECL(mp_vc_c4)
 MP_VH_DECL(mp_vb_c1)
 MP_VH_DECL(mp_vb_c3)
@@ -29,6 +31,10 @@ int mp_vh_code(int cin, int cmid, int radius)
     if (cmid == 1 && (cin == 1 || cin == 3 || cin == 4)) code = cin;
     else if (cmid == cin && (cin == 3 || cin == 4)) code = 4 + cin;
     if (code < 0 || radius < 1 || radius > MP_VH_RBIG) return -1;
+    // RGB channel-preserving radii 1..4 and 5..8 run on their own kernels
+    // (code + 64, code + 128)
+    if (code == 7 && radius <= 4) return code + 64;
+    if (code == 7 && radius <= 8) return code + 128;
     if (radius <= MP_VH_RMAX) return code;
     // buckets: channel-keeping kernels only (1-channel source, RGB, RGBA)
     return (code == 1 || code == 7 || code == 8) ? code + 16 : -1;
@@ -36,7 +42,7 @@ int mp_vh_code(int cin, int cmid, int radius)
 
 int mp_vh_dot_code(int c, int radius)
 {
-    const int code = mp_vh_code(c, c, radius);
+    const int code = mp_vh_code(c, c, radius) & 63;   // the dot mode has one kernel for every radius
     return (code == 1 || code == 7 || code == 8) ? code + 32 : -1;
 }
 
@@ -52,6 +58,8 @@ static const void *mp_vh_fn(int code, bool single)
     case 3: return single ? (const void *)mp_vh_c3_single : (const void *)mp_vh_c3_batch;
     case 4: return single ? (const void *)mp_vh_c4_single : (const void *)mp_vh_c4_batch;
     case 7: return single ? (const void *)mp_vc_c3_single : (const void *)mp_vc_c3_batch;
+    case 7 + 64: return single ? (const void *)mp_vc_c3_lo_single : (const void *)mp_vc_c3_lo_batch;
+    case 7 + 128: return single ? (const void *)mp_vc_c3_mid_single : (const void *)mp_vc_c3_mid_batch;
     case 8: return single ? (const void *)mp_vc_c4_single : (const void *)mp_vc_c4_batch;
     case 17: return single ? (const void *)mp_vb_c1_single : (const void *)mp_vb_c1_batch;
     case 23: return single ? (const void *)mp_vb_c3_single : (const void *)mp_vb_c3_batch;

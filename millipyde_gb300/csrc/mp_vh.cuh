@@ -581,6 +581,45 @@ __device__ __forceinline__ void vh_dispatch(const MPJob &J, int lt, float *smem,
     }
 }
 
+// Radius groups of the exact-radius kernels, compiled as separate kernels
+// so that each is allocated registers for its own radii (smaller radii:
+// smaller windows, more resident CTAs per SM): 1..4, 5..8, 9..12.
+template <int CIN, int CM>
+__device__ __forceinline__ void vh_dispatch_lo(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
+{
+    switch (J.radius) {
+#define MP_VH_CASE(RR) \
+    case RR: vh_item<CIN, CM, RR>(J, lt, smem, gc, err); break;
+        MP_VH_CASE(1) MP_VH_CASE(2) MP_VH_CASE(3) MP_VH_CASE(4)
+#undef MP_VH_CASE
+    default: break;
+    }
+}
+
+template <int CIN, int CM>
+__device__ __forceinline__ void vh_dispatch_mid(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
+{
+    switch (J.radius) {
+#define MP_VH_CASE(RR) \
+    case RR: vh_item<CIN, CM, RR>(J, lt, smem, gc, err); break;
+        MP_VH_CASE(5) MP_VH_CASE(6) MP_VH_CASE(7) MP_VH_CASE(8)
+#undef MP_VH_CASE
+    default: break;
+    }
+}
+
+template <int CIN, int CM>
+__device__ __forceinline__ void vh_dispatch_hi(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
+{
+    switch (J.radius) {
+#define MP_VH_CASE(RR) \
+    case RR: vh_item<CIN, CM, RR>(J, lt, smem, gc, err); break;
+        MP_VH_CASE(9) MP_VH_CASE(10) MP_VH_CASE(11) MP_VH_CASE(12)
+#undef MP_VH_CASE
+    default: break;
+    }
+}
+
 // The d sigma dot mode, radii 1..MP_VH_RMAX.
 template <int CIN, int CM>
 __device__ __forceinline__ void vh_dispatch_dot(const MPJob &J, int lt, float *smem, uint32_t &gc, int *err)
@@ -661,6 +700,11 @@ __device__ __forceinline__ void vh_init(float *smem)
 // larger window needs the registers, the wider strip keeps the halo share
 // down).
 #define MP_VH_KERNELS(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch, 3, MP_VH_NT)
+// Radius groups (see vh_dispatch_lo): 4 resident CTAs per SM for radii up to
+// 8, 3 above.
+#define MP_VH_KERNELS_LO(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_lo, 4, MP_VH_NT)
+#define MP_VH_KERNELS_MID(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_mid, 4, MP_VH_NT)
+#define MP_VH_KERNELS_HI(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_hi, 3, MP_VH_NT)
 #define MP_VH_KERNELS_BIG(NAME, CIN, CM) MP_VH_KERNELS_X(NAME, CIN, CM, vh_dispatch_big, 1, MP_VH_NT_BIG)
 #ifndef MP_VH_DOT_MINB
 #define MP_VH_DOT_MINB 3
