@@ -717,7 +717,7 @@ def bench_ingest(torch):
     pinned = best(lambda: px.to("cuda", non_blocking=True))
     return {"bytes": nb, "gpuimage_from_ndarray_gbs": round(h2d, 1), "ndarray_from_gpuimage_gbs": round(d2h, 1),
             "torch_pageable_h2d_gbs": round(pageable, 1), "torch_pinned_h2d_gbs": round(pinned, 1),
-            "path": "library objects: page-locked staging in 16 MB chunks for copies from 4 MB"}
+            "path": "library objects: one copy straight from pageable memory (2-D for pitched rows)"}
 
 
 # ----------------------------------------------------------------- main GPU run

@@ -53,11 +53,13 @@ def _plan_tiles(L, spec_stages, nst, xs, seed):
 def test_tuned_geometry_changes_the_plan_and_stays_exact(gpu, clean):
     L = clean
     rng = np.random.default_rng(41)
+    # one streaming-gaussian launch big enough that rows per work item are
+    # not at their floor (32 rows)
+    big = [rng.random((900, 900, 3), dtype=np.float32) for _ in range(12)]
+    gstages = _abi.stages(_abi.stage("gaussian", 2.0))
     xs = [rng.random((int(h), int(w), 3), dtype=np.float32)
           for h, w in rng.integers(40, 700, size=(10, 2))]
-    stages = _abi.stages(*[_abi.stage(d["op"], random=d.get("random", False), lo=d.get("lo"), hi=d.get("hi"),
-                                      probability=d.get("probability", -1.0)) for d in RAGGED])
-    base = dict(_plan_tiles(L, stages, 4, xs, 5))
+    base = dict(_plan_tiles(L, gstages, 1, big, 0))
     settings = [(8, 0, 1), (8, 0, 16), (8, 2, 64), (8, 1, 1), (5, 1, 1)]
     for kind, param, value in settings:
         L.mpk_tune_clear()
@@ -65,10 +67,11 @@ def test_tuned_geometry_changes_the_plan_and_stays_exact(gpu, clean):
         got = C.c_int()
         _abi.check(L.mpk_tune_get_kernel(kind, param, C.byref(got)))
         assert got.value == value
-        tiles = dict(_plan_tiles(L, stages, 4, xs, 5))
+        tiles = dict(_plan_tiles(L, gstages, 1, big, 0))
         if (kind, param) in ((8, 0), (8, 2)):
             # work items of the streaming gaussian follow the setting
             assert tiles[8] != base[8], (kind, param, value, tiles, base)
+        check_spec([dict(op="gaussian", lo=(2.0,))], big[:2])
         check_spec(RAGGED, xs, seed=5)
 
 

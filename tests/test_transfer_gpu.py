@@ -1,11 +1,7 @@
 """GPU: object transfers between host arrays and device objects.
 
-Copies of 4 MB and more go through two page-locked staging chunks (16 MB
-each) so the host copy of one chunk overlaps the DMA of the other; smaller
-copies go direct.  Every layout must round-trip exactly: pitched image rows
-(row bytes not a multiple of 16), packed rows, 1-D arrays, bytes, chunk
-boundaries that fall inside and between rows, and sizes just under and just
-over one chunk."""
+Every layout must round-trip exactly: pitched image rows (row bytes not a
+multiple of 16), packed rows, byte images, 1-D arrays, large and small."""
 import numpy as np
 import pytest
 
@@ -17,12 +13,12 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("shape,dtype", [
-    ((2000, 1801, 3), np.float32),     # pitched rows, 43 MB: three chunks
-    ((1200, 1200, 3), np.float32),     # packed rows (14400 B), 17 MB: one chunk and a tail
+    ((2000, 1801, 3), np.float32),     # pitched rows, 43 MB
+    ((1200, 1200, 3), np.float32),     # packed rows (14400 B), 17 MB
     ((3000, 2001, 4), np.uint8),       # pitched byte rows, 24 MB
-    ((300, 301, 3), np.float32),       # 1 MB: the direct path
-    ((4 << 20,), np.float32),          # 1-D, exactly one chunk
-    ((5_000_001,), np.float32),        # 1-D, just over one chunk
+    ((300, 301, 3), np.float32),       # 1 MB
+    ((4 << 20,), np.float32),          # 1-D, 16 MB
+    ((5_000_001,), np.float32),        # 1-D, odd length
 ])
 def test_roundtrip_through_the_c_abi(gpu, shape, dtype):
     rng = np.random.default_rng(sum(shape))
