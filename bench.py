@@ -405,8 +405,11 @@ def bench_ragged(args, torch, L, uuid, cpu_pool):
             h2d += h * w * 12
             d2h += h * w * 12
         hia, hoa = _abi.images(hins), _abi.images(houts)
-        _abi.check(L.mpk_pipeline_run_host(st, len(RAGGED_SPEC), hia, hoa, n, SEED, 0, sp))
-        e2e_steps = max(1, min(3, args.steps))
+        # the first calls of the host path are slower (first DMA from fresh
+        # page-locked pages, pool growth): three warm-up calls
+        for _ in range(3):
+            _abi.check(L.mpk_pipeline_run_host(st, len(RAGGED_SPEC), hia, hoa, n, SEED, 0, sp))
+        e2e_steps = max(1, min(5, args.steps))
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             _abi.check(L.mpk_pipeline_run_host(st, len(RAGGED_SPEC), hia, hoa, n, SEED, 0, sp))

@@ -362,7 +362,7 @@ MPStatus mpk_tune_get_gauss_tile(int cin, int cmid, int has_pro, int radius, int
  * after the prologue (1, 3 or 4). */
 MPStatus mpk_tune_set_stream(int cmid, int stages);
 /* Intermediate bytes one chunk of a fused batch may hold (at least 1 MB;
- * default 512 MB): a batch runs as one launch per segment per chunk. */
+ * default 2 GB): a batch runs as one launch per segment per chunk. */
 MPStatus mpk_tune_set_chunk_bytes(size_t bytes);
 /* Geometry of the persistent kernels, per launch kind (5 footprint rotate,
  * 8 streaming gaussian, 9 fused gaussian + rotate); value 0 restores the

@@ -26,10 +26,11 @@
 
 // Intermediate bytes a chunk of a fused batch may hold (one launch per
 // segment per chunk; mpk_tune_set_chunk_bytes changes it).  Measured on
-// GB300 (256 x 1024^2 RGB, grey -> gaussian -> rotate -> gamma): 48 MB
-// chunks (intermediates small enough for L2) 2.33 ms per step, 512 MB
-// chunks 1.49 ms -- fewer, longer launches win over L2 residency.
-static size_t mp_chunk_bytes = (size_t)512 << 20;
+// GB300: the uniform batch (256 x 1024^2 RGB) took 2.33 ms per step with
+// 48 MB chunks and 1.49 ms with 512 MB; the ragged batch (1000 RGB images,
+// 4 GB of intermediates) 6.59 ms with 512 MB and 6.06 ms with 2 GB (8 GB:
+// the same) -- fewer, longer launches win over L2 residency.
+static size_t mp_chunk_bytes = (size_t)2048 << 20;
 
 struct ROp {
     int op;
@@ -1866,6 +1867,12 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     }
     const int nslots = chunks.size() > 1 ? 2 : 1;
     void *ibuf[2] = {nullptr, nullptr}, *obuf[2] = {nullptr, nullptr};
+    // Packed landing buffers: an image whose host rows are packed crosses
+    // the link as one 1-D copy and is re-pitched device to device (and the
+    // reverse for results).  Measured on GB300: 2-D host-to-device copies
+    // of 1.5 KB rows ran at 35 GB/s (21 GB/s per 129-row image), of 6.9 KB
+    // rows at 107 GB/s, a 1-D copy at 212 GB/s.
+    void *lin[2] = {nullptr, nullptr}, *lout[2] = {nullptr, nullptr};
     std::vector<MPPlan *> plans(chunks.size(), nullptr);
     cudaEvent_t ev[4][2];
     bool ev_ok = true;
@@ -1877,6 +1884,8 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     for (int s = 0; s < nslots && st == MILLIPYDE_SUCCESS; ++s) {
         st = mp_malloc_async(&ibuf[s], max_in, cs);
         if (st == MILLIPYDE_SUCCESS) st = mp_malloc_async(&obuf[s], max_out, cs);
+        if (st == MILLIPYDE_SUCCESS) st = mp_malloc_async(&lin[s], max_in, cs);
+        if (st == MILLIPYDE_SUCCESS) st = mp_malloc_async(&lout[s], max_out, cs);
     }
     // every plan is created (and its job table uploaded) before any copy is
     // queued, so the host never waits on the compute stream inside the loop
@@ -1897,11 +1906,24 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     for (size_t k = 0; k < chunks.size() && st == MILLIPYDE_SUCCESS; ++k) {
         const int slot = (int)(k % nslots), f = chunks[k].first, c = chunks[k].second;
         if (k >= (size_t)nslots) cudaStreamWaitEvent(hs, ev[E_COMP][slot], 0);   // input slot free
-        for (int i = f; i < f + c && st == MILLIPYDE_SUCCESS; ++i)
-            if (din[i].height > 0 && din[i].width > 0)
-                st = mp_cuda_status(cudaMemcpy2DAsync(din[i].data, din[i].pitch, in[i].data, in[i].pitch,
-                                                      (size_t)in[i].width * in[i].channels * 4,
-                                                      in[i].height, cudaMemcpyHostToDevice, hs));
+        for (int i = f; i < f + c && st == MILLIPYDE_SUCCESS; ++i) {
+            if (din[i].height <= 0 || din[i].width <= 0) continue;
+            const size_t rb = (size_t)in[i].width * in[i].channels * 4, h = (size_t)in[i].height;
+            if ((size_t)in[i].pitch == (size_t)din[i].pitch) {
+                // same row pitch on both sides: the rows and their padding in one copy
+                st = mp_cuda_status(cudaMemcpyAsync(din[i].data, in[i].data, (h - 1) * (size_t)in[i].pitch + rb,
+                                                    cudaMemcpyHostToDevice, hs));
+            } else if ((size_t)in[i].pitch == rb) {
+                void *land = (char *)lin[slot] + in_off[i];
+                st = mp_cuda_status(cudaMemcpyAsync(land, in[i].data, h * rb, cudaMemcpyHostToDevice, hs));
+                if (st == MILLIPYDE_SUCCESS)
+                    st = mp_cuda_status(cudaMemcpy2DAsync(din[i].data, din[i].pitch, land, rb, rb, h,
+                                                          cudaMemcpyDeviceToDevice, hs));
+            } else {
+                st = mp_cuda_status(cudaMemcpy2DAsync(din[i].data, din[i].pitch, in[i].data, in[i].pitch, rb, h,
+                                                      cudaMemcpyHostToDevice, hs));
+            }
+        }
         if (st != MILLIPYDE_SUCCESS) break;
         cudaEventRecord(ev[E_H2D][slot], hs);
         cudaStreamWaitEvent(cs, ev[E_H2D][slot], 0);
@@ -1910,11 +1932,20 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
         if (st != MILLIPYDE_SUCCESS) break;
         cudaEventRecord(ev[E_COMP][slot], cs);
         cudaStreamWaitEvent(ds, ev[E_COMP][slot], 0);
-        for (int i = f; i < f + c && st == MILLIPYDE_SUCCESS; ++i)
-            if (dout[i].height > 0 && dout[i].width > 0)
-                st = mp_cuda_status(cudaMemcpy2DAsync(out[i].data, out[i].pitch, dout[i].data, dout[i].pitch,
-                                                      (size_t)dout[i].width * dout[i].channels * 4,
-                                                      dout[i].height, cudaMemcpyDeviceToHost, ds));
+        for (int i = f; i < f + c && st == MILLIPYDE_SUCCESS; ++i) {
+            if (dout[i].height <= 0 || dout[i].width <= 0) continue;
+            const size_t rb = (size_t)dout[i].width * dout[i].channels * 4, h = (size_t)dout[i].height;
+            if ((size_t)out[i].pitch == rb && (size_t)dout[i].pitch != rb) {
+                void *land = (char *)lout[slot] + out_off[i];
+                st = mp_cuda_status(cudaMemcpy2DAsync(land, rb, dout[i].data, dout[i].pitch, rb, h,
+                                                      cudaMemcpyDeviceToDevice, ds));
+                if (st == MILLIPYDE_SUCCESS)
+                    st = mp_cuda_status(cudaMemcpyAsync(out[i].data, land, h * rb, cudaMemcpyDeviceToHost, ds));
+            } else {
+                st = mp_cuda_status(cudaMemcpy2DAsync(out[i].data, out[i].pitch, dout[i].data, dout[i].pitch, rb, h,
+                                                      cudaMemcpyDeviceToHost, ds));
+            }
+        }
         cudaEventRecord(ev[E_D2H][slot], ds);
     }
     cudaStreamSynchronize(hs);
@@ -1922,6 +1953,8 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     cudaStreamSynchronize(cs);
     for (MPPlan *p : plans) mpk_plan_destroy(p);
     for (int s = 0; s < 2; ++s) {
+        mp_free_async(lin[s], cs);
+        mp_free_async(lout[s], cs);
         mp_free_async(ibuf[s], cs);
         mp_free_async(obuf[s], cs);
     }
