@@ -1868,7 +1868,7 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     const int nslots = chunks.size() > 1 ? 2 : 1;
     void *ibuf[2] = {nullptr, nullptr}, *obuf[2] = {nullptr, nullptr};
     // Packed landing buffers: an image whose host rows are packed crosses
-    // the link as one 1-D copy and is re-pitched device to device (and the
+    // the link as one 1-D copy and is re-pitched on the device (and the
     // reverse for results).  Measured on GB300: 2-D host-to-device copies
     // of 1.5 KB rows ran at 35 GB/s (21 GB/s per 129-row image), of 6.9 KB
     // rows at 107 GB/s, a 1-D copy at 212 GB/s.
@@ -1888,15 +1888,43 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
         if (st == MILLIPYDE_SUCCESS) st = mp_malloc_async(&lout[s], max_out, cs);
     }
     // every plan is created (and its job table uploaded) before any copy is
-    // queued, so the host never waits on the compute stream inside the loop
+    // queued, so the host never waits on the compute stream inside the loop.
+    // Images whose host rows are packed but whose device pitch differs land
+    // packed and are re-pitched by an identity plan (the copy kernel) on the
+    // copy stream, in both directions, so the copy engines carry only the
+    // link's bytes.
+    std::vector<MPPlan *> rin(chunks.size(), nullptr), rout(chunks.size(), nullptr);
+    auto land_in = [&](int i) { return (size_t)in[i].pitch == (size_t)in[i].width * in[i].channels * 4 &&
+                                       in[i].pitch != din[i].pitch && din[i].height > 0 && din[i].width > 0; };
+    auto land_out = [&](int i) { return (size_t)out[i].pitch == (size_t)dout[i].width * dout[i].channels * 4 &&
+                                        out[i].pitch != dout[i].pitch && dout[i].height > 0 && dout[i].width > 0; };
     for (size_t k = 0; k < chunks.size() && st == MILLIPYDE_SUCCESS; ++k) {
         const int slot = (int)(k % nslots), f = chunks[k].first, c = chunks[k].second;
+        std::vector<MPImage> ls, ld, ms, md;
         for (int i = f; i < f + c; ++i) {
             din[i].data = (char *)ibuf[slot] + in_off[i];
             dout[i].data = (char *)obuf[slot] + out_off[i];
+            if (land_in(i)) {
+                MPImage l = din[i];
+                l.data = (char *)lin[slot] + in_off[i];
+                l.pitch = in[i].pitch;
+                ls.push_back(l);
+                ld.push_back(din[i]);
+            }
+            if (land_out(i)) {
+                MPImage l = dout[i];
+                l.data = (char *)lout[slot] + out_off[i];
+                l.pitch = out[i].pitch;
+                ms.push_back(dout[i]);
+                md.push_back(l);
+            }
         }
         st = mpk_plan_create(stages, nstages, &din[f], &dout[f], c, seed, index0 + (uint64_t)f, cs,
                              &plans[k]);
+        if (st == MILLIPYDE_SUCCESS && !ls.empty())
+            st = mpk_plan_create(nullptr, 0, ls.data(), ld.data(), (int)ls.size(), 0, 0, cs, &rin[k]);
+        if (st == MILLIPYDE_SUCCESS && !ms.empty())
+            st = mpk_plan_create(nullptr, 0, ms.data(), md.data(), (int)ms.size(), 0, 0, cs, &rout[k]);
     }
     if (st == MILLIPYDE_SUCCESS) {
         st = mp_cuda_status(cudaEventRecord(ev[E_ALLOC][0], cs));
@@ -1913,17 +1941,15 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
                 // same row pitch on both sides: the rows and their padding in one copy
                 st = mp_cuda_status(cudaMemcpyAsync(din[i].data, in[i].data, (h - 1) * (size_t)in[i].pitch + rb,
                                                     cudaMemcpyHostToDevice, hs));
-            } else if ((size_t)in[i].pitch == rb) {
-                void *land = (char *)lin[slot] + in_off[i];
-                st = mp_cuda_status(cudaMemcpyAsync(land, in[i].data, h * rb, cudaMemcpyHostToDevice, hs));
-                if (st == MILLIPYDE_SUCCESS)
-                    st = mp_cuda_status(cudaMemcpy2DAsync(din[i].data, din[i].pitch, land, rb, rb, h,
-                                                          cudaMemcpyDeviceToDevice, hs));
+            } else if (land_in(i)) {
+                st = mp_cuda_status(cudaMemcpyAsync((char *)lin[slot] + in_off[i], in[i].data, h * rb,
+                                                    cudaMemcpyHostToDevice, hs));
             } else {
                 st = mp_cuda_status(cudaMemcpy2DAsync(din[i].data, din[i].pitch, in[i].data, in[i].pitch, rb, h,
                                                       cudaMemcpyHostToDevice, hs));
             }
         }
+        if (st == MILLIPYDE_SUCCESS && rin[k]) st = mpk_plan_launch(rin[k], hs);
         if (st != MILLIPYDE_SUCCESS) break;
         cudaEventRecord(ev[E_H2D][slot], hs);
         cudaStreamWaitEvent(cs, ev[E_H2D][slot], 0);
@@ -1932,15 +1958,13 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
         if (st != MILLIPYDE_SUCCESS) break;
         cudaEventRecord(ev[E_COMP][slot], cs);
         cudaStreamWaitEvent(ds, ev[E_COMP][slot], 0);
+        if (st == MILLIPYDE_SUCCESS && rout[k]) st = mpk_plan_launch(rout[k], ds);
         for (int i = f; i < f + c && st == MILLIPYDE_SUCCESS; ++i) {
             if (dout[i].height <= 0 || dout[i].width <= 0) continue;
             const size_t rb = (size_t)dout[i].width * dout[i].channels * 4, h = (size_t)dout[i].height;
-            if ((size_t)out[i].pitch == rb && (size_t)dout[i].pitch != rb) {
-                void *land = (char *)lout[slot] + out_off[i];
-                st = mp_cuda_status(cudaMemcpy2DAsync(land, rb, dout[i].data, dout[i].pitch, rb, h,
-                                                      cudaMemcpyDeviceToDevice, ds));
-                if (st == MILLIPYDE_SUCCESS)
-                    st = mp_cuda_status(cudaMemcpyAsync(out[i].data, land, h * rb, cudaMemcpyDeviceToHost, ds));
+            if (land_out(i)) {
+                st = mp_cuda_status(cudaMemcpyAsync(out[i].data, (char *)lout[slot] + out_off[i], h * rb,
+                                                    cudaMemcpyDeviceToHost, ds));
             } else {
                 st = mp_cuda_status(cudaMemcpy2DAsync(out[i].data, out[i].pitch, dout[i].data, dout[i].pitch, rb, h,
                                                       cudaMemcpyDeviceToHost, ds));
@@ -1952,6 +1976,8 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     cudaStreamSynchronize(ds);
     cudaStreamSynchronize(cs);
     for (MPPlan *p : plans) mpk_plan_destroy(p);
+    for (MPPlan *p : rin) mpk_plan_destroy(p);
+    for (MPPlan *p : rout) mpk_plan_destroy(p);
     for (int s = 0; s < 2; ++s) {
         mp_free_async(lin[s], cs);
         mp_free_async(lout[s], cs);

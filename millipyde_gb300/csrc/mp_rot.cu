@@ -186,55 +186,6 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
         }
         return;
     }
-    if constexpr (C > 1 && EK != RO_EPI_LIST) {
-        // several channels: two pixels (rows RSTEP apart) per step in packed
-        // pairs, each channel lerped as a + f (b - a)
-        const float2 sc = make_float2(1.1920928955078125e-7f, 1.1920928955078125e-7f);
-        const float2 m1 = make_float2(-1.0f, -1.0f);
-#pragma unroll
-        for (int i = 0; i < NPX; i += 2) {
-            const int lxb = lx + stx, lyb = ly + sty;
-            const float2 fx = ro_fma2(make_float2(ro_frac_bits(lx), ro_frac_bits(lxb)), sc, m1);
-            const float2 fy = ro_fma2(make_float2(ro_frac_bits(ly), ro_frac_bits(lyb)), sc, m1);
-            const float *pa = buf + (ly >> 24) * bxw + (lx >> 24) * C + delta;
-            const float *pb = buf + (lyb >> 24) * bxw + (lxb >> 24) * C + delta;
-            float o0[C], o1[C];
-#pragma unroll
-            for (int k = 0; k < C; ++k) {
-                const float2 a = make_float2(pa[k], pb[k]), b = make_float2(pa[C + k], pb[C + k]);
-                const float2 c = make_float2(pa[bxw + k], pb[bxw + k]), d = make_float2(pa[bxw + C + k], pb[bxw + C + k]);
-                const float2 v0 = ro_fma2(fx, ro_sub2(b, a), a);
-                const float2 v1 = ro_fma2(fx, ro_sub2(d, c), c);
-                const float2 v = ro_fma2(fy, ro_sub2(v1, v0), v0);
-                float x0 = v.x, x1 = v.y;
-                const bool colour = !(C == 4 && k == 3);   // alpha passes untouched
-                if (EK == RO_EPI_GAMMA && colour) {
-                    x0 = mp_clamp01(e1 * __powf(x0, e0));
-                    x1 = mp_clamp01(e1 * __powf(x1, e0));
-                } else if (EK == RO_EPI_BRIGHT && colour) {
-                    x0 = mp_clamp01(x0 + e0);
-                    x1 = mp_clamp01(x1 + e0);
-                } else if (EK == RO_EPI_ONE) {
-                    x0 = mp_pw_chan(epi.op, epi.p0, epi.p1, epi.p2, x0, k, C);
-                    x1 = mp_pw_chan(epi.op, epi.p0, epi.p1, epi.p2, x1, k, C);
-                }
-                o0[k] = x0;
-                o1[k] = x1;
-            }
-            if (full || yf + RSTEP * i < ho) {
-#pragma unroll
-                for (int k = 0; k < C; ++k) drow[k] = o0[k];
-            }
-            if (full || yf + RSTEP * (i + 1) < ho) {
-#pragma unroll
-                for (int k = 0; k < C; ++k) drow[rstride + k] = o1[k];
-            }
-            lx = lxb + stx;
-            ly = lyb + sty;
-            drow += 2 * rstride;
-        }
-        return;
-    }
 #pragma unroll
     for (int i = 0; i < NPX; ++i) {
         if (full || yf + RSTEP * i < ho) {
