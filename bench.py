@@ -409,18 +409,26 @@ def bench_ragged(args, torch, L, uuid, cpu_pool):
         # page-locked pages, pool growth): three warm-up calls
         for _ in range(3):
             _abi.check(L.mpk_pipeline_run_host(st, len(RAGGED_SPEC), hia, hoa, n, SEED, 0, sp))
-        e2e_steps = max(1, min(5, args.steps))
-        t0 = time.perf_counter()
+        # each step timed on its own: the median is the value, every step's
+        # time is listed (occasional steps several times slower than the rest
+        # come from the host: bare copies of the same bytes show them too)
+        e2e_steps = max(1, min(7, args.steps))
+        step_s = []
         for _ in range(e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
             _abi.check(L.mpk_pipeline_run_host(st, len(RAGGED_SPEC), hia, hoa, n, SEED, 0, sp))
-        e2e_s = (time.perf_counter() - t0) / e2e_steps
+            step_s.append(time.perf_counter() - t0)
+        e2e_s = statistics.median(step_s)
         i0 = check[0]
         h, w = sizes[i0]
         d = float((hkeep[2 * i0 + 1] - keep[2 * i0 + 1][:, : w * 3].cpu()).abs().max())
         if not d <= 1e-6:
             raise SystemExit("bench.py: host-buffer path differs from the device path by %.3g" % d)
         out["e2e"] = {"value": round(px / 1e6 / e2e_s, 1), "unit": "Mpix/s", "h2d_bytes_per_step": h2d,
-                      "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                      "d2h_bytes_per_step": d2h, "steps": e2e_steps, "statistic": "median step",
+                      "steps_ms": [round(1e3 * t, 2) for t in step_s],
+                      "mean_value": round(px / 1e6 / statistics.mean(step_s), 1),
                       "path": "mpk_pipeline_run_host, page-locked host buffers"}
         del hkeep
         # CPU baseline: the oracle port on the host cores, every 8th image
