@@ -381,18 +381,7 @@ MPStatus mpk_tune_get_kernel(int kind, int param, int *value);
  * The autotuner times both and records the faster.  Plans created
  * afterwards follow the setting. */
 MPStatus mpk_tune_set_fuse(int enable);
-/* Pipelined plans: a batch whose images run two or more segments is cut
- * into chunks of at most chunk_bytes of intermediates; segment j of each
- * chunk runs on one of two streams, after segment j - 1 of the same chunk,
- * so the next chunk's first stage overlaps this chunk's second stage and
- * the intermediate is read back while still in L2 (intermediates rotate
- * through three scratch slots).  0 (the default): one stream, chunks of the
- * size mpk_tune_set_chunk_bytes sets.  Plans created afterwards follow it;
- * their launches stay ordered on the stream they are launched (or captured)
- * on. */
-MPStatus mpk_tune_set_pipeline(size_t chunk_bytes);
-/* Clears the tuned tables and restores the defaults (fusion off, no
- * pipelined plans). */
+/* Clears the tuned tables and restores the defaults (fusion off). */
 void mpk_tune_clear(void);
 
 /* Differentiable chains on dense batches (the autograd path): B images of

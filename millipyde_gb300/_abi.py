@@ -134,7 +134,6 @@ SIGNATURES = {
     "mpk_tune_set_stream": (_ST, [C.c_int] * 2),
     "mpk_tune_set_chunk_bytes": (_ST, [C.c_size_t]),
     "mpk_tune_set_fuse": (_ST, [C.c_int]),
-    "mpk_tune_set_pipeline": (_ST, [C.c_size_t]),
     "mpk_tune_set_kernel": (_ST, [C.c_int, C.c_int, C.c_int]),
     "mpk_tune_get_kernel": (_ST, [C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "mpk_tune_clear": (None, []),

@@ -54,15 +54,6 @@ struct Seg {
 // timings of both).
 static int mp_fuse_mode = 0;
 
-// Pipelined plans (mpk_tune_set_pipeline): a batch whose images run two or
-// more segments is cut into chunks of at most this many intermediate bytes;
-// segment j of chunk c runs on stream j % 2 of the plan, after segment j - 1
-// of chunk c, so the second stage of one chunk overlaps the first stage of
-// the next, and a chunk's intermediate is read back while it is still in
-// L2.  Intermediates rotate through MP_PIPE_SLOTS scratch slots.  0: off.
-static size_t mp_pipe_chunk = 0;
-#define MP_PIPE_SLOTS 3
-
 // Tuned geometry of the persistent kernels per launch kind (5 footprint
 // rotate, 8 streaming gaussian, 9 fused gaussian + rotate), set by the
 // autotuner through mpk_tune_set_kernel; 0 keeps the built-in choice.
@@ -637,21 +628,10 @@ struct MPLaunch {
     int grid;       // GSTREAM: persistent CTAs
     FzGeom fz;      // FUSE: shared-memory geometry
     int fz_cin;     // FUSE: source channels
-    int chunk, seg; // chunk of the plan and segment index of the launch
-};
-
-// Launches [first, first + count) of a plan form segment `seg` of chunk
-// `chunk` (pipelined plans order their streams by these groups).
-struct MPSegRun {
-    int chunk, seg, last_seg, first, count;
 };
 
 struct MPPlanImpl {
     std::vector<MPLaunch> launches;
-    std::vector<MPSegRun> runs;            // pipelined plans: segment groups in launch order
-    bool pipelined = false;
-    cudaStream_t side = nullptr;           // pipelined plans: the second stream
-    std::vector<cudaEvent_t> events;       // pipelined plans: one per segment group, then start / end
     void *tables = nullptr;    // one device block: job table, then tile -> job map
     MPJob *jobs_dev = nullptr;
     int *tiles_dev = nullptr;
@@ -1165,10 +1145,6 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
     struct Chunk { std::vector<int> imgs; };
     std::vector<Chunk> chunks;
     size_t scratch_need = 0;
-    // pipelined when enabled and some image runs two or more segments
-    bool pipe = false;
-    if (mp_pipe_chunk > 0)
-        for (int i = 0; i < nimgs; ++i) pipe = pipe || segs[i].size() >= 2;
     {
         size_t i = 0;
         while (i < order.size()) {
@@ -1183,7 +1159,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 size_t b = 0;
                 for (size_t k = 0; k + 1 < sg.size(); ++k)
                     b += (size_t)sg[k].hout * mp_round16((long long)sg[k].wout * sg[k].cout * 4);
-                if (!ch.imgs.empty() && bytes + b > (pipe ? mp_pipe_chunk : mp_chunk_bytes)) break;
+                if (!ch.imgs.empty() && bytes + b > mp_chunk_bytes) break;
                 bytes += b;
                 ch.imgs.push_back(order[i]);
                 ++i;
@@ -1192,19 +1168,13 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             chunks.push_back(ch);
         }
     }
-    // 3. scratch for intermediates (reused by every chunk, stream-ordered;
-    //    pipelined plans rotate through MP_PIPE_SLOTS slots)
-    const size_t slot_bytes = (scratch_need + 255) / 256 * 256;
-    const int nslots = pipe ? MP_PIPE_SLOTS : 1;
-    MPStatus st = mp_malloc_async(&P->scratch, slot_bytes * nslots, s);
+    // 3. scratch for intermediates (reused by every chunk, stream-ordered)
+    MPStatus st = mp_malloc_async(&P->scratch, scratch_need, s);
     if (st != MILLIPYDE_SUCCESS) return st;
-    P->pipelined = pipe;
-    int chunk_id = 0;
     // 4. jobs
     MPTables T;
     for (const Chunk &ch : chunks) {
         const size_t nseg = segs[ch.imgs[0]].size();
-        char *slot_base = (char *)P->scratch + (size_t)(chunk_id % nslots) * slot_bytes;
         // intermediate images of this chunk
         std::vector<std::vector<MPImage>> inter(ch.imgs.size(), std::vector<MPImage>(nseg));
         size_t off = 0;
@@ -1216,14 +1186,12 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 m.width = sg[k].wout;
                 m.channels = sg[k].cout;
                 m.pitch = mp_round16((long long)m.width * m.channels * 4);
-                m.data = slot_base + off;
+                m.data = (char *)P->scratch + off;
                 off += (size_t)m.height * m.pitch;
                 inter[q][k] = m;
             }
         }
-        std::vector<size_t> seg_start(nseg + 1);
         for (size_t k = 0; k < nseg; ++k) {
-            seg_start[k] = P->launches.size();
             // uniform tile geometry for this launch
             int kind = segs[ch.imgs[0]][k].kind;
             int tw = 0, th = 0;
@@ -1285,29 +1253,6 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             st = T.add(P->launches, kind, mp_seg_variant(segs[ch.imgs[0]][k]), smem, js, bytes);
             if (st != MILLIPYDE_SUCCESS) return st;
         }
-        seg_start[nseg] = P->launches.size();
-        for (size_t k = 0; k < nseg; ++k) {
-            for (size_t i = seg_start[k]; i < seg_start[k + 1]; ++i) {
-                P->launches[i].chunk = chunk_id;
-                P->launches[i].seg = (int)k;
-            }
-            P->runs.push_back({chunk_id, (int)k, (int)nseg - 1, (int)seg_start[k], (int)(seg_start[k + 1] - seg_start[k])});
-        }
-        ++chunk_id;
-    }
-    if (pipe) {
-        // the two stages of neighbouring chunks share the SMs: the streaming
-        // gaussian keeps at most 2 CTAs per SM and the footprint rotate 1
-        // (tuned caps take precedence)
-        for (MPLaunch &L : P->launches) {
-            int cap = 0;
-            if (L.kind == MPK_VH) cap = mp_tuned(MPK_VH, MP_TK_CTAS) > 0 ? mp_tuned(MPK_VH, MP_TK_CTAS) : 2;
-            if (L.kind == MPK_RSTREAM) cap = mp_tuned(MPK_RSTREAM, MP_TK_CTAS) > 0 ? mp_tuned(MPK_RSTREAM, MP_TK_CTAS) : 1;
-            if (cap > 0) L.grid = std::min(L.grid, cap * mp_num_sms());
-        }
-        MP_CUDA_TRY(cudaStreamCreateWithFlags(&P->side, cudaStreamNonBlocking));
-        P->events.assign(P->runs.size() + 2, nullptr);
-        for (cudaEvent_t &e : P->events) MP_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     return mp_plan_finish(P, T, s);
 }
@@ -1339,44 +1284,8 @@ static MPStatus mp_plan_launch_one(const MPPlanImpl *P, size_t idx, cudaStream_t
                           L.smem, P->err, s, L.gauss);
 }
 
-// Pipelined plan: segment j of chunk c on stream j % 2 (s or the plan's
-// side stream), after segment j - 1 of chunk c; segment 0 of chunk c after
-// the last segment of chunk c - MP_PIPE_SLOTS (its scratch slot).  The side
-// stream joins s at the start and s waits for it at the end, so the whole
-// plan is ordered on s (and can be captured from s).
-static MPStatus mp_plan_launch_pipelined(const MPPlanImpl *P, cudaStream_t s)
-{
-    const size_t nr = P->runs.size();
-    cudaEvent_t start = P->events[nr], end = P->events[nr + 1];
-    MP_CUDA_TRY(cudaEventRecord(start, s));
-    MP_CUDA_TRY(cudaStreamWaitEvent(P->side, start, 0));
-    std::vector<int> chunk_last;   // run index of each chunk's last segment
-    for (size_t r = 0; r < nr; ++r) {
-        const MPSegRun &R = P->runs[r];
-        cudaStream_t st = (R.seg % 2 == 0) ? s : P->side;
-        if (R.seg > 0) {
-            MP_CUDA_TRY(cudaStreamWaitEvent(st, P->events[r - 1], 0));
-        } else if (R.chunk >= MP_PIPE_SLOTS) {
-            MP_CUDA_TRY(cudaStreamWaitEvent(st, P->events[chunk_last[R.chunk - MP_PIPE_SLOTS]], 0));
-        }
-        for (int i = R.first; i < R.first + R.count; ++i) {
-            MPStatus e = mp_plan_launch_one(P, (size_t)i, st);
-            if (e != MILLIPYDE_SUCCESS) return e;
-        }
-        MP_CUDA_TRY(cudaEventRecord(P->events[r], st));
-        if (R.seg == R.last_seg) {
-            if ((int)chunk_last.size() <= R.chunk) chunk_last.resize(R.chunk + 1, 0);
-            chunk_last[R.chunk] = (int)r;
-        }
-    }
-    MP_CUDA_TRY(cudaEventRecord(end, P->side));
-    MP_CUDA_TRY(cudaStreamWaitEvent(s, end, 0));
-    return MILLIPYDE_SUCCESS;
-}
-
 static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
 {
-    if (P->pipelined) return mp_plan_launch_pipelined(P, s);
     for (size_t i = 0; i < P->launches.size(); ++i) {
         MPStatus st = mp_plan_launch_one(P, i, s);
         if (st != MILLIPYDE_SUCCESS) return st;
@@ -1386,11 +1295,6 @@ static MPStatus mp_plan_launch(const MPPlanImpl *P, cudaStream_t s)
 
 static void mp_plan_free(MPPlanImpl *P, cudaStream_t s)
 {
-    for (cudaEvent_t e : P->events)
-        if (e) cudaEventDestroy(e);
-    P->events.clear();
-    if (P->side) cudaStreamDestroy(P->side);
-    P->side = nullptr;
     mp_free_async(P->tables, s);
     mp_free_async(P->scratch, s);
     mp_free_async(P->counters, s);
@@ -2682,13 +2586,6 @@ extern "C" MPStatus mpk_tune_get_kernel(int kind, int param, int *value)
     return MILLIPYDE_SUCCESS;
 }
 
-extern "C" MPStatus mpk_tune_set_pipeline(size_t chunk_bytes)
-{
-    if (chunk_bytes != 0 && chunk_bytes < ((size_t)1 << 20)) return MP_ERROR_INVALID_ARGS;
-    mp_pipe_chunk = chunk_bytes;
-    return MILLIPYDE_SUCCESS;
-}
-
 extern "C" MPStatus mpk_tune_set_fuse(int enable)
 {
     if (enable != 0 && enable != 1) return MP_ERROR_INVALID_ARGS;
@@ -2698,7 +2595,6 @@ extern "C" MPStatus mpk_tune_set_fuse(int enable)
 
 extern "C" void mpk_tune_clear(void)
 {
-    mp_pipe_chunk = 0;
     {
         std::lock_guard<std::mutex> lk(mp_ktune_mutex);
         memset(mp_ktune, 0, sizeof(mp_ktune));
