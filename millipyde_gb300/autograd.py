@@ -65,23 +65,30 @@ def _opcodes(names):
     return arr
 
 
-# Host tables of per-image parameters, reused while the parameter tensors
-# are the same live objects with unchanged version counters: the planner
-# needs the values on the host (taps, rotation constants, footprints), and
-# reading device tensors synchronises the device, so a forward whose
-# parameters have not been written since the last one queues its launches
-# without waiting for the previous step.  (Writes through `.data` bypass the
-# version counter; write parameters in place under torch.no_grad(), as
-# optimisers do.)
+# Host tables of per-image parameters, reused while the device parameter
+# tensors are the same live objects with unchanged version counters and the
+# host parameters (python floats, CPU tensors) have the same values: the
+# planner needs the values on the host (taps, rotation constants,
+# footprints), and reading device tensors synchronises the device, so a
+# forward whose parameters have not been written since the last one queues
+# its launches without waiting for the previous step.  (Writes through
+# `.data` bypass the version counter; write parameters in place under
+# torch.no_grad(), as optimisers do.)
 _PCACHE = []
 _PCACHE_MAX = 8
 
 
 def _param_table(B, nops, slots, ptensors):
-    vers = [t._version for t in ptensors]
-    for key, refs, P in _PCACHE:
-        if key == (B, nops, tuple(slots), tuple(vers)) and len(refs) == len(ptensors) and \
-                all(r() is t for r, t in zip(refs, ptensors)):
+    sig, dev_t = [], []
+    for t in ptensors:
+        if t.device.type == "cpu":
+            sig.append(tuple(t.detach().reshape(-1).tolist()))
+        else:
+            sig.append(t._version)
+            dev_t.append(t)
+    key = (B, nops, tuple(slots), tuple(sig))
+    for k, refs, P in _PCACHE:
+        if k == key and len(refs) == len(dev_t) and all(r() is t for r, t in zip(refs, dev_t)):
             return P
     P = torch.zeros((B, max(1, nops), 3), dtype=torch.float64)
     cols = {}
@@ -98,7 +105,7 @@ def _param_table(B, nops, slots, ptensors):
         P[:, k, j] = cols[i]
     if len(_PCACHE) >= _PCACHE_MAX:
         _PCACHE.pop(0)
-    _PCACHE.append(((B, nops, tuple(slots), tuple(vers)), [weakref.ref(t) for t in ptensors], P))
+    _PCACHE.append((key, [weakref.ref(t) for t in dev_t], P))
     return P
 
 
@@ -141,7 +148,12 @@ class _ChainFn(torch.autograd.Function):
                                                gy.data_ptr(), dx.data_ptr(), dP.data_ptr(), mask,
                                                B, H, W, Cc, stream))
         grads = []
-        for (k, j), (shape, dtype, dev) in zip(ctx.slots, ctx.pshapes):
+        for i, ((k, j), (shape, dtype, dev)) in enumerate(zip(ctx.slots, ctx.pshapes)):
+            if not ctx.needs_input_grad[3 + i]:
+                # no gradient wanted (e.g. a constant python float): none is
+                # formed, and none is copied to a host tensor
+                grads.append(None)
+                continue
             g = dP[:, k, j]
             g = g.sum().reshape(shape) if len(shape) == 0 or shape.numel() == 1 and B != 1 else g.reshape(shape)
             grads.append(g.to(device=dev, dtype=dtype))

@@ -2190,6 +2190,21 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
     }
     for (int k = 0; k <= nops; ++k) gmax = std::max(gmax, (size_t)sh[k].h * sh[k].w * sh[k].c * 4);
     const size_t per_img = inter + 2 * gmax;
+    // intermediates the reverse sweep reads: the input of each pointwise
+    // run (grouped as the sweep groups them), of a gaussian whose sigma
+    // wants a gradient (the d sigma dot passes) and of every rotate (d theta,
+    // and the gather adjoint's source geometry); transpose and fliplr read
+    // none.  The recompute stops at the last of them.
+    int last_needed = 0;
+    for (int k = nops - 1; k >= 0;) {
+        int j = k;
+        if (mp_is_pointwise(ops[k]))
+            while (j > 0 && mp_is_pointwise(ops[j - 1]) && k - (j - 1) < MP_MAX_PW) --j;
+        const bool reads = mp_is_pointwise(ops[k]) || ops[k] == MP_OP_ROTATE ||
+                           (ops[k] == MP_OP_GAUSSIAN && wants(k));
+        if (reads) last_needed = std::max(last_needed, j);
+        k = j - 1;
+    }
     int chunk = (int)std::max<size_t>(1, MP_BWD_SCRATCH_BYTES / std::max<size_t>(per_img, 1));
     chunk = std::min(chunk, B);
     void *scratch = nullptr;
@@ -2242,8 +2257,9 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
             }
             return MILLIPYDE_SUCCESS;
         };
-        // ---- forward recompute: a_{k+1} = op_k(a_k), k = 0..n-2
-        for (int k = 0; k + 1 < nops && st == MILLIPYDE_SUCCESS; ++k) {
+        // ---- forward recompute: a_{k+1} = op_k(a_k), up to the last
+        //      intermediate an adjoint pass reads
+        for (int k = 0; k < last_needed && st == MILLIPYDE_SUCCESS; ++k) {
             std::vector<MPJob> js;
             size_t smem = 0;
             const int kind = seg_of(0, k).kind;

@@ -39,6 +39,13 @@
 #define MP_VH_NT 128       // threads of a CTA (2 columns each)
 #define MP_VH_NT_BIG 256   // threads of the radius-bucket kernels: wider strips, the halo a smaller share
 #define MP_VH_VR 8
+// Largest radius at which the channel-preserving family pairs output rows
+// in the horizontal pass (one f32x2 FMA per tap for two rows).  Measured on
+// interleaved RGB: radii 1..4 about 5 % faster paired; 5..8 spill at the
+// 128-register budget of their kernel and 9..12 ran 7 % slower.
+#ifndef MP_VH_PAIR_RMAX
+#define MP_VH_PAIR_RMAX 4
+#endif
 
 namespace mp_vh {
 
@@ -144,8 +151,9 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     constexpr int NTAP = 2 * R + 1, RC = R * CM, R4 = (RC + 3) & ~3, E = R4 - RC;
     constexpr int NW2 = BIG ? R + 1 : NTAP;               // tap registers
     // the plain one-channel family computes two output rows per
-    // horizontal work item as packed pairs
-    constexpr bool PAIR = CM == 1 && !BIG && !DOT;
+    // horizontal work item as packed pairs, and so does the channel-
+    // preserving family up to radius MP_VH_PAIR_RMAX
+    constexpr bool PAIR = (CM == 1 || R <= MP_VH_PAIR_RMAX) && !BIG && !DOT;
     constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
     constexpr int D = R8 - R;                             // tap offset inside the window
     constexpr int NWIN = VR + 2 * R8;

@@ -19,3 +19,16 @@ def test_table_reused_while_unchanged_and_rebuilt_after_writes():
     # a new tensor object with other values is never mistaken for the old one
     p3 = A._param_table(2, 2, slots, [torch.tensor([1.0, 2.0], dtype=torch.float64), sigma])
     assert p3[:, 0, 0].tolist() == [1.0, 2.0]
+
+
+def test_host_parameters_match_by_value():
+    """Python floats become a new CPU tensor on every call (adjust_gamma's
+    implicit gain among them): equal values reuse the table, other values
+    do not."""
+    gamma = torch.tensor([0.8, 1.2], dtype=torch.float64)
+    slots = [(0, 0), (0, 1)]
+    p1 = A._param_table(2, 1, slots, [gamma, torch.tensor(1.0, dtype=torch.float64)])
+    assert A._param_table(2, 1, slots, [gamma, torch.tensor(1.0, dtype=torch.float64)]) is p1
+    p2 = A._param_table(2, 1, slots, [gamma, torch.tensor(0.5, dtype=torch.float64)])
+    assert p2 is not p1 and p2[:, 0, 1].tolist() == [0.5, 0.5]
+    assert p1[:, 0, 1].tolist() == [1.0, 1.0]
