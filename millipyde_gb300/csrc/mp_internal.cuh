@@ -420,6 +420,9 @@ mp_encode_tiled_fn mp_get_encode_tiled();
 // Stream-ordered allocation from the device's memory pool.
 MPStatus mp_malloc_async(void **p, size_t bytes, cudaStream_t s);
 void mp_free_async(void *p, cudaStream_t s);
+// Host-to-device copy of a host table that the caller may reuse as soon as
+// this returns (staged through a page-locked ring: no wait for the stream).
+MPStatus mp_upload_async(void *dst, const void *src, size_t bytes, cudaStream_t s);
 
 // Kernel launchers (mp_kernels.cu).  `jobs` is a device table of njobs jobs
 // sorted by tile0; `total_tiles` the sum of their ntiles.

@@ -708,7 +708,7 @@ struct MPTables {
         if (st != MILLIPYDE_SUCCESS) return st;
         P->jobs_dev = (MPJob *)P->tables;
         P->tiles_dev = (int *)((unsigned char *)P->tables + jb);
-        return mp_cuda_status(cudaMemcpyAsync(P->tables, host.data(), jb + tb, cudaMemcpyHostToDevice, s));
+        return mp_upload_async(P->tables, host.data(), jb + tb, s);
     }
 };
 

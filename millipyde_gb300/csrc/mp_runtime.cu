@@ -10,7 +10,9 @@
 // has one non-blocking library stream that objects are ordered on.
 #include <algorithm>
 #include <atomic>
+#include <deque>
 #include <mutex>
+#include <vector>
 #include <string.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -272,6 +274,111 @@ MPStatus mp_malloc_async(void **p, size_t bytes, cudaStream_t s)
     const size_t lim = mp_alloc_limit.load();
     if (lim && bytes > lim) return MP_ERROR_OUT_OF_MEMORY;
     return mp_cuda_status(cudaMallocAsync(p, bytes, s));
+}
+
+// ---------------------------------------------------------------------------
+// Host-to-device uploads of plan tables through a page-locked ring.  A copy
+// from pageable memory may wait for the stream's earlier work before it
+// starts (the driver stages it through its own page-locked buffer), which
+// would serialise the host's planning of the next batch with the device's
+// execution of the last.  The ring is one page-locked block per device,
+// handed out in order; a slot is reused only after the event recorded
+// behind its copy has completed, which by then it normally has (a whole lap
+// of uploads later).  Uploads while the stream is being captured, and
+// uploads larger than a quarter of the ring, copy directly: a captured copy
+// from the ring would replay whatever the slot holds later.
+// ---------------------------------------------------------------------------
+#define MP_RING_BYTES ((size_t)32 << 20)
+
+struct MPRingSlot {
+    size_t off, bytes;
+    unsigned long long lap;
+    cudaEvent_t ev;
+};
+
+struct MPRing {
+    unsigned char *base = nullptr;
+    bool failed = false;
+    size_t head = 0;
+    unsigned long long lap = 0;
+    std::deque<MPRingSlot> busy;      // oldest first
+    std::vector<cudaEvent_t> spare;
+};
+
+static std::mutex mp_ring_mutex;
+static MPRing mp_rings[MP_MAX_DEVICES];
+
+static MPStatus mp_ring_retire(MPRing &R, const MPRingSlot &sl)
+{
+    MP_CUDA_TRY(cudaEventSynchronize(sl.ev));
+    R.spare.push_back(sl.ev);
+    return MILLIPYDE_SUCCESS;
+}
+
+MPStatus mp_upload_async(void *dst, const void *src, size_t bytes, cudaStream_t s)
+{
+    if (bytes == 0) return MILLIPYDE_SUCCESS;
+    int d = 0;
+    cudaGetDevice(&d);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        cs = cudaStreamCaptureStatusActive;
+    }
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    if (cs != cudaStreamCaptureStatusNone || d < 0 || d >= MP_MAX_DEVICES || need > MP_RING_BYTES / 4)
+        return mp_cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    std::lock_guard<std::mutex> lk(mp_ring_mutex);
+    MPRing &R = mp_rings[d];
+    if (!R.base && !R.failed) {
+        if (cudaHostAlloc((void **)&R.base, MP_RING_BYTES, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            R.base = nullptr;
+            R.failed = true;
+        }
+    }
+    if (!R.base) return mp_cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+    if (R.head + need > MP_RING_BYTES) {
+        // wrap: the previous lap's slots past this lap's end are retired
+        // now, so that only this lap's slots (in offset order) stay queued
+        while (!R.busy.empty() && R.busy.front().lap < R.lap) {
+            MPStatus st = mp_ring_retire(R, R.busy.front());
+            R.busy.pop_front();
+            if (st != MILLIPYDE_SUCCESS) return st;
+        }
+        R.head = 0;
+        ++R.lap;
+    }
+    const size_t lo = R.head, hi = R.head + need;
+    while (!R.busy.empty() && R.busy.front().lap < R.lap && R.busy.front().off < hi) {
+        MPStatus st = mp_ring_retire(R, R.busy.front());
+        R.busy.pop_front();
+        if (st != MILLIPYDE_SUCCESS) return st;
+    }
+    cudaEvent_t ev = nullptr;
+    if (!R.spare.empty()) {
+        ev = R.spare.back();
+        R.spare.pop_back();
+    } else {
+        MP_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    memcpy(R.base + lo, src, bytes);
+    cudaError_t e = cudaMemcpyAsync(dst, R.base + lo, bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        R.spare.push_back(ev);
+        return mp_cuda_status(e);
+    }
+    e = cudaEventRecord(ev, s);
+    if (e != cudaSuccess) {
+        // the copy is queued but nothing marks its end: wait for it before
+        // the slot can be handed out again
+        R.spare.push_back(ev);
+        cudaStreamSynchronize(s);
+        return mp_cuda_status(e);
+    }
+    R.busy.push_back(MPRingSlot{lo, need, R.lap, ev});
+    R.head = hi;
+    return MILLIPYDE_SUCCESS;
 }
 
 extern "C" MPStatus mpdev_pool_usage(int device_id, uint64_t *reserved, uint64_t *used, uint64_t *used_peak)

@@ -59,6 +59,8 @@ def test_tuned_geometry_changes_the_plan_and_stays_exact(gpu, clean):
     gstages = _abi.stages(_abi.stage("gaussian", 2.0))
     xs = [rng.random((int(h), int(w), 3), dtype=np.float32)
           for h, w in rng.integers(40, 700, size=(10, 2))]
+    # the built-in geometry (the loaded table may already set some knobs)
+    L.mpk_tune_clear()
     base = dict(_plan_tiles(L, gstages, 1, big, 0))
     settings = [(8, 0, 1), (8, 0, 16), (8, 2, 64), (8, 1, 1), (5, 1, 1)]
     for kind, param, value in settings:
