@@ -403,6 +403,23 @@ MPStatus mpk_chain_backward(const int *ops, int nops, const double *params, cons
 MPStatus mpk_chain_backward_masked(const int *ops, int nops, const double *params, const float *x,
                                    const float *dy, float *dx, double *dparams, const int *param_mask,
                                    int B, int H, int W, int C, void *stream);
+/* Saved forward intermediates: the forward plan writes the input a_k of
+ * every op k that opens one of its later segments anyway; with a saved
+ * block the forward writes them there and the backward reads them instead
+ * of recomputing them (it recomputes only the intermediates it needs that
+ * were not saved, starting from the nearest saved one).  Layout for B
+ * images: *count entries (at most nops); entry s is a_{op_index[s]}, B dense
+ * images (rows of w*c floats, shape from the chain) from byte offset[s];
+ * *bytes is the whole block (0: nothing is saved for this chain).  The
+ * layout depends on the op kinds and shapes only.  op_index / offset may
+ * be null.  The block must stay untouched between the two calls. */
+MPStatus mpk_chain_saved_layout(const int *ops, int nops, int B, int H, int W, int C, int *count,
+                                int *op_index, size_t *offset, size_t *bytes);
+MPStatus mpk_chain_forward_saved(const int *ops, int nops, const double *params, const float *x, float *y,
+                                 void *saved, int B, int H, int W, int C, void *stream);
+MPStatus mpk_chain_backward_saved(const int *ops, int nops, const double *params, const float *x,
+                                  const void *saved, const float *dy, float *dx, double *dparams,
+                                  const int *param_mask, int B, int H, int W, int C, void *stream);
 
 /* Allocation-free batch.  No counterpart in the reference.  For callers that
  * cannot allocate device memory (GPU memory owned by another allocator or

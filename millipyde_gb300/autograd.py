@@ -9,10 +9,11 @@ or (B, C, H, W) with channels_first=True.  Each op parameter is a python
 float (same for every image) or a tensor of shape (B,) (per image; may
 require grad).  adjust_gamma takes (gamma[, gain]), colorize (r, g, b).
 
-Forward runs the fused batch path (mpk_chain_forward).  Backward
-(mpk_chain_backward) saves nothing but x and the parameters: it recomputes
-the forward intermediates image chunk by image chunk (bounded scratch) and
-runs the adjoints in reverse -- one pass for each run of pointwise ops
+Forward runs the fused batch path (mpk_chain_forward_saved) and, when a
+backward will follow, keeps the intermediates the fused plan writes anyway
+(the inputs of its later segments).  Backward (mpk_chain_backward_saved)
+reads those, recomputes the other intermediates it needs image chunk by
+image chunk (bounded scratch) and runs the adjoints in reverse -- one pass for each run of pointwise ops
 (with their parameter gradients), blur(g) and, when sigma requires grad, two
 derivative-tap dot passes for gaussian (d sigma), the exact transpose of the bilinear gather plus
 d theta for rotate, and the inverse permutation for transpose / fliplr.
@@ -122,8 +123,20 @@ class _ChainFn(torch.autograd.Function):
         _abi.check(L.mpk_chain_shape(ops, nops, H, W, Cc, C.byref(ho), C.byref(wo), C.byref(co)))
         y = torch.empty((B, ho.value, wo.value, co.value), device=x.device, dtype=torch.float32)
         stream = torch.cuda.current_stream(x.device).cuda_stream
-        _abi.check(L.mpk_chain_forward(ops, nops, P.data_ptr(), x.data_ptr(), y.data_ptr(),
-                                       B, H, W, Cc, stream))
+        # with a backward to come, the forward keeps the intermediates it
+        # writes anyway (segment boundaries) so that the backward does not
+        # recompute them
+        saved = None
+        if any(ctx.needs_input_grad):
+            cnt, nbytes = C.c_int(), C.c_size_t()
+            _abi.check(L.mpk_chain_saved_layout(ops, nops, B, H, W, Cc, C.byref(cnt), None, None,
+                                                C.byref(nbytes)))
+            if nbytes.value:
+                saved = torch.empty(nbytes.value, dtype=torch.uint8, device=x.device)
+        _abi.check(L.mpk_chain_forward_saved(ops, nops, P.data_ptr(), x.data_ptr(), y.data_ptr(),
+                                             saved.data_ptr() if saved is not None else None,
+                                             B, H, W, Cc, stream))
+        ctx.saved_inter = saved
         ctx.save_for_backward(x)
         ctx.P, ctx.names, ctx.slots, ctx.nparams = P, names, slots, len(ptensors)
         ctx.pshapes = [(t.shape, t.dtype, t.device) for t in ptensors]
@@ -144,9 +157,12 @@ class _ChainFn(torch.autograd.Function):
         for i, (k, _) in enumerate(ctx.slots):
             if ctx.needs_input_grad[3 + i]:
                 mask[k] = 1
-        _abi.check(L.mpk_chain_backward_masked(_opcodes(ctx.names), nops, ctx.P.data_ptr(), x.data_ptr(),
-                                               gy.data_ptr(), dx.data_ptr(), dP.data_ptr(), mask,
-                                               B, H, W, Cc, stream))
+        sv = ctx.saved_inter
+        _abi.check(L.mpk_chain_backward_saved(_opcodes(ctx.names), nops, ctx.P.data_ptr(), x.data_ptr(),
+                                              sv.data_ptr() if sv is not None else None,
+                                              gy.data_ptr(), dx.data_ptr(), dP.data_ptr(), mask,
+                                              B, H, W, Cc, stream))
+        ctx.saved_inter = None
         grads = []
         for i, ((k, j), (shape, dtype, dev)) in enumerate(zip(ctx.slots, ctx.pshapes)):
             if not ctx.needs_input_grad[3 + i]:

@@ -47,6 +47,7 @@ struct Seg {
     int hin, win, hout, wout;
     double rot_angle;   // FUSE: the rotate's angle (core_p holds the gaussian's sigma)
     PwList epi2;        // FUSE: the gaussian's epilogue
+    int op0;            // index of the op that opened the segment (its input is a_op0)
 };
 
 // Fusion of a one-channel gaussian with the rotate after it (MPK_FUSE):
@@ -165,7 +166,8 @@ static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
     cur.hin = cur.hout = h;
     cur.win = cur.wout = w;
     int c = cin;
-    for (const ROp &r : ops) {
+    for (size_t oi = 0; oi < ops.size(); ++oi) {
+        const ROp &r = ops[oi];
         if (mp_is_pointwise(r.op)) {
             // identity cases: grey of a 1-channel image, colorize of a grey image
             if (r.op == MP_OP_RGB2GREY && c < 3) continue;
@@ -181,6 +183,7 @@ static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
                 nx.cin = nx.cmid = nx.cout = c;
                 nx.hin = nx.hout = cur.hout;
                 nx.win = nx.wout = cur.wout;
+                nx.op0 = (int)oi;
                 cur = nx;
                 mp_pw_push(cur.pro, r);
             } else {
@@ -203,6 +206,7 @@ static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
             nx.cin = nx.cmid = nx.cout = c;
             nx.hin = nx.hout = cur.hout;
             nx.win = nx.wout = cur.wout;
+            nx.op0 = (int)oi;
             cur = nx;
         }
         cur.core_op = r.op;
@@ -1090,10 +1094,21 @@ static MPStatus mp_plan_finish(MPPlanImpl *P, MPTables &T, cudaStream_t s)
     return mp_cuda_status(cudaMemsetAsync(P->counters, 0, cb, s));
 }
 
+// Caller-provided homes for a plan's intermediates (the saved forward
+// intermediates of a differentiable chain): image i's output of segment s
+// (s below its last) is written to at[i][s] when at[i][s].data is set, and
+// takes no scratch.  Plans with homes skip fusion, so that every segment
+// boundary stays materialised.
+struct MPInterHomes {
+    std::vector<std::vector<MPImage>> at;
+    bool has(int i, size_t s) const { return i < (int)at.size() && s < at[i].size() && at[i][s].data; }
+};
+
 static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage *in,
                               const MPImage *out, int nimgs, uint64_t seed, uint64_t index0,
                               cudaStream_t s, MPPlanImpl *P,
-                              const std::vector<std::vector<ROp>> *explicit_ops = nullptr)
+                              const std::vector<std::vector<ROp>> *explicit_ops = nullptr,
+                              const MPInterHomes *homes = nullptr)
 {
     if (nimgs < 0 || nstages < 0 || (nimgs > 0 && (!in || !out)) ||
         (nstages > 0 && !stages && !explicit_ops))
@@ -1121,7 +1136,7 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
             if (st != MILLIPYDE_SUCCESS) return st;
         }
         mp_segment(ops, in[i].channels, in[i].height, in[i].width, segs[i]);
-        mp_fuse_segments(segs[i], in[i]);
+        if (!homes) mp_fuse_segments(segs[i], in[i]);
         const Seg &last = segs[i].back();
         if (!out[i].data && (long long)last.hout * last.wout > 0) return MP_ERROR_NULL_DATA;
         if (out[i].height != last.hout || out[i].width != last.wout ||
@@ -1158,7 +1173,8 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
                 if (!same) break;
                 size_t b = 0;
                 for (size_t k = 0; k + 1 < sg.size(); ++k)
-                    b += (size_t)sg[k].hout * mp_round16((long long)sg[k].wout * sg[k].cout * 4);
+                    if (!homes || !homes->has(order[i], k))
+                        b += (size_t)sg[k].hout * mp_round16((long long)sg[k].wout * sg[k].cout * 4);
                 if (!ch.imgs.empty() && bytes + b > mp_chunk_bytes) break;
                 bytes += b;
                 ch.imgs.push_back(order[i]);
@@ -1181,6 +1197,10 @@ static MPStatus mp_plan_build(const MPStage *stages, int nstages, const MPImage 
         for (size_t q = 0; q < ch.imgs.size(); ++q) {
             const auto &sg = segs[ch.imgs[q]];
             for (size_t k = 0; k + 1 < nseg; ++k) {
+                if (homes && homes->has(ch.imgs[q], k)) {
+                    inter[q][k] = homes->at[ch.imgs[q]][k];
+                    continue;
+                }
                 MPImage m;
                 m.height = sg[k].hout;
                 m.width = sg[k].wout;
@@ -2050,8 +2070,56 @@ extern "C" MPStatus mpk_chain_shape(const int *ops, int nops, int H, int W, int 
     return MILLIPYDE_SUCCESS;
 }
 
-extern "C" MPStatus mpk_chain_forward(const int *ops, int nops, const double *params, const float *x,
-                                      float *y, int B, int H, int W, int C, void *stream)
+// Saved forward intermediates of a chain: the inputs a_k of the ops that
+// open the forward plan's second and later segments (the intermediates the
+// fused forward writes anyway).  Entry s is a_{idx[s]}, B dense images
+// (rows of w*c floats) from byte off[s] of the saved block.  Segmentation
+// depends on the op kinds and channels only, so any parameters give the
+// same layout.
+static void mp_chain_saved_layout(const int *ops, int nops, int B, const std::vector<MPShape> &sh,
+                                  std::vector<int> &idx, std::vector<size_t> &off, size_t *total)
+{
+    std::vector<ROp> kinds(nops);
+    for (int k = 0; k < nops; ++k) {
+        memset(&kinds[k], 0, sizeof(ROp));
+        kinds[k].op = ops[k];
+    }
+    std::vector<Seg> segs;
+    mp_segment(kinds, sh[0].c, sh[0].h, sh[0].w, segs);
+    idx.clear();
+    off.clear();
+    size_t t = 0;
+    for (size_t q = 1; q < segs.size(); ++q) {
+        const int k = segs[q].op0;
+        idx.push_back(k);
+        off.push_back(t);
+        t += (size_t)B * sh[k].h * sh[k].w * sh[k].c * 4;
+    }
+    *total = t;
+}
+
+extern "C" MPStatus mpk_chain_saved_layout(const int *ops, int nops, int B, int H, int W, int C, int *count,
+                                           int *op_index, size_t *offset, size_t *bytes)
+{
+    if (B < 0 || (nops > 0 && !ops) || !count) return MP_ERROR_INVALID_ARGS;
+    std::vector<MPShape> sh;
+    MPStatus st = mp_chain_shapes(ops, nops, H, W, C, sh);
+    if (st != MILLIPYDE_SUCCESS) return st;
+    std::vector<int> idx;
+    std::vector<size_t> off;
+    size_t total = 0;
+    mp_chain_saved_layout(ops, nops, B, sh, idx, off, &total);
+    *count = (int)idx.size();
+    for (size_t i = 0; i < idx.size(); ++i) {
+        if (op_index) op_index[i] = idx[i];
+        if (offset) offset[i] = off[i];
+    }
+    if (bytes) *bytes = total;
+    return MILLIPYDE_SUCCESS;
+}
+
+extern "C" MPStatus mpk_chain_forward_saved(const int *ops, int nops, const double *params, const float *x,
+                                            float *y, void *saved, int B, int H, int W, int C, void *stream)
 {
     if (B < 0 || (B > 0 && (!x || !y || (nops > 0 && (!ops || !params))))) return MP_ERROR_INVALID_ARGS;
     std::vector<MPShape> sh;
@@ -2064,13 +2132,30 @@ extern "C" MPStatus mpk_chain_forward(const int *ops, int nops, const double *pa
         out[b] = mp_dense_image(y, b, sh.back());
         for (int k = 0; k < nops; ++k) per[b].push_back(mp_rop(ops[k], params + ((size_t)b * nops + k) * 3));
     }
+    MPInterHomes homes;
+    if (saved) {
+        std::vector<int> idx;
+        std::vector<size_t> off;
+        size_t total = 0;
+        mp_chain_saved_layout(ops, nops, B, sh, idx, off, &total);
+        homes.at.assign(B, std::vector<MPImage>(idx.size()));
+        for (int b = 0; b < B; ++b)
+            for (size_t q = 0; q < idx.size(); ++q)
+                homes.at[b][q] = mp_dense_image((const float *)((const char *)saved + off[q]), b, sh[idx[q]]);
+    }
     MPPlanImpl P;
     cudaGetDevice(&P.device);
     P.stream = (cudaStream_t)stream;
-    st = mp_plan_build(nullptr, 0, in.data(), out.data(), B, 0, 0, P.stream, &P, &per);
+    st = mp_plan_build(nullptr, 0, in.data(), out.data(), B, 0, 0, P.stream, &P, &per, saved ? &homes : nullptr);
     if (st == MILLIPYDE_SUCCESS) st = mp_plan_launch(&P, P.stream);
     mp_plan_free(&P, P.stream);
     return st;
+}
+
+extern "C" MPStatus mpk_chain_forward(const int *ops, int nops, const double *params, const float *x,
+                                      float *y, int B, int H, int W, int C, void *stream)
+{
+    return mpk_chain_forward_saved(ops, nops, params, x, y, nullptr, B, H, W, C, stream);
 }
 
 // Derivative of the normalised gaussian taps with respect to sigma:
@@ -2160,6 +2245,14 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
                                               const float *dy, float *dx, double *dparams, const int *param_mask,
                                               int B, int H, int W, int C, void *stream)
 {
+    return mpk_chain_backward_saved(ops, nops, params, x, nullptr, dy, dx, dparams, param_mask, B, H, W, C,
+                                    stream);
+}
+
+extern "C" MPStatus mpk_chain_backward_saved(const int *ops, int nops, const double *params, const float *x,
+                                             const void *saved, const float *dy, float *dx, double *dparams,
+                                             const int *param_mask, int B, int H, int W, int C, void *stream)
+{
     // param_mask[k] != 0: the parameters of op k want a gradient (null: all ops)
     auto wants = [&](int k) { return dparams && (!param_mask || param_mask[k] != 0); };
     if (B < 0 || (B > 0 && (!x || !dy || !dx || (nops > 0 && (!ops || !params)))))
@@ -2181,30 +2274,53 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
         return mp_cuda_status(cudaMemcpyAsync(dx, dy, (size_t)B * H * W * C * 4,
                                               cudaMemcpyDeviceToDevice, s));
     }
-    // scratch per image: intermediates a_1..a_{n-1} + two gradient buffers
-    size_t inter = 0, gmax = 0;
-    std::vector<size_t> aoff(nops + 1, 0);
-    for (int k = 1; k < nops; ++k) {
-        aoff[k] = inter;
-        inter += (size_t)sh[k].h * sh[k].w * sh[k].c * 4;
+    // intermediates the forward saved (a_k of the saved layout), if any
+    std::vector<long long> saved_off(nops + 1, -1);
+    if (saved) {
+        std::vector<int> idx;
+        std::vector<size_t> off;
+        size_t total = 0;
+        mp_chain_saved_layout(ops, nops, B, sh, idx, off, &total);
+        for (size_t q = 0; q < idx.size(); ++q) saved_off[idx[q]] = (long long)off[q];
     }
-    for (int k = 0; k <= nops; ++k) gmax = std::max(gmax, (size_t)sh[k].h * sh[k].w * sh[k].c * 4);
-    const size_t per_img = inter + 2 * gmax;
     // intermediates the reverse sweep reads: the input of each pointwise
     // run (grouped as the sweep groups them), of a gaussian whose sigma
     // wants a gradient (the d sigma dot passes) and of every rotate (d theta,
     // and the gather adjoint's source geometry); transpose and fliplr read
-    // none.  The recompute stops at the last of them.
-    int last_needed = 0;
+    // none.
+    std::vector<char> need(nops + 1, 0);
     for (int k = nops - 1; k >= 0;) {
         int j = k;
         if (mp_is_pointwise(ops[k]))
             while (j > 0 && mp_is_pointwise(ops[j - 1]) && k - (j - 1) < MP_MAX_PW) --j;
         const bool reads = mp_is_pointwise(ops[k]) || ops[k] == MP_OP_ROTATE ||
                            (ops[k] == MP_OP_GAUSSIAN && wants(k));
-        if (reads) last_needed = std::max(last_needed, j);
+        if (reads) need[j] = 1;
         k = j - 1;
     }
+    // recompute a_{k+1} = op_k(a_k) for k in [rc0, rc1): from the last saved
+    // (or the input) at or below the first needed intermediate that was not
+    // saved, up to the last one; saved intermediates inside the range are
+    // read, not recomputed
+    int rc0 = 0, rc1 = 0, lo_unsaved = -1;
+    for (int k = 1; k < nops; ++k)
+        if (need[k] && saved_off[k] < 0) {
+            if (lo_unsaved < 0) lo_unsaved = k;
+            rc1 = k;
+        }
+    if (lo_unsaved > 0)
+        for (int k = 1; k <= lo_unsaved; ++k)
+            if (saved_off[k] >= 0) rc0 = k;
+    // scratch per image: the intermediates recomputed here + two gradient buffers
+    size_t inter = 0, gmax = 0;
+    std::vector<size_t> aoff(nops + 1, 0);
+    for (int k = rc0 + 1; k <= rc1; ++k) {
+        if (saved_off[k] >= 0) continue;
+        aoff[k] = inter;
+        inter += (size_t)sh[k].h * sh[k].w * sh[k].c * 4;
+    }
+    for (int k = 0; k <= nops; ++k) gmax = std::max(gmax, (size_t)sh[k].h * sh[k].w * sh[k].c * 4);
+    const size_t per_img = inter + 2 * gmax;
     int chunk = (int)std::max<size_t>(1, MP_BWD_SCRATCH_BYTES / std::max<size_t>(per_img, 1));
     chunk = std::min(chunk, B);
     void *scratch = nullptr;
@@ -2216,6 +2332,8 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
         // per-image pointers inside the chunk's scratch
         auto a_img = [&](int q, int k) -> MPImage {       // input of op k for image b0+q
             if (k == 0) return mp_dense_image(x, b0 + q, sh[0]);
+            if (saved_off[k] >= 0)
+                return mp_dense_image((const float *)((const char *)saved + saved_off[k]), b0 + q, sh[k]);
             MPImage m = mp_dense_image((const float *)(sbase + (size_t)q * per_img + aoff[k]), 0, sh[k]);
             return m;
         };
@@ -2257,9 +2375,9 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
             }
             return MILLIPYDE_SUCCESS;
         };
-        // ---- forward recompute: a_{k+1} = op_k(a_k), up to the last
-        //      intermediate an adjoint pass reads
-        for (int k = 0; k < last_needed && st == MILLIPYDE_SUCCESS; ++k) {
+        // ---- forward recompute of the intermediates the adjoints read
+        for (int k = rc0; k < rc1 && st == MILLIPYDE_SUCCESS; ++k) {
+            if (saved_off[k + 1] >= 0) continue;
             std::vector<MPJob> js;
             size_t smem = 0;
             const int kind = seg_of(0, k).kind;

@@ -145,3 +145,33 @@ def test_chain_backward_masked_host_checks():
     bad = (C.c_int * 1)(99)
     assert f(bad, 1, params, None, None, None, None, mask, 0, 8, 8, 3, None) == _abi.MP_ERROR_BAD_DESCRIPTOR
     assert f(ops, 2, params, None, None, None, None, mask, 0, 8, 8, 3, None) == _abi.MILLIPYDE_SUCCESS
+
+
+def test_chain_saved_layout():
+    """Saved forward intermediates of a differentiable chain: the inputs of
+    the ops that open the forward plan's later segments (host arithmetic
+    only, no device call)."""
+    import ctypes as C
+    from millipyde_gb300 import _abi
+    L = _abi.lib()
+
+    def layout(names, B=2, H=5, W=4, Cc=3):
+        codes = {"rotate": _abi.OP_ROTATE, "gaussian": _abi.OP_GAUSSIAN, "adjust_gamma": _abi.OP_ADJUST_GAMMA,
+                 "rgb2grey": _abi.OP_RGB2GREY, "brightness": _abi.OP_BRIGHTNESS,
+                 "transpose": _abi.OP_TRANSPOSE, "fliplr": _abi.OP_FLIPLR}
+        n = len(names)
+        ops = (C.c_int * max(1, n))(*[codes[x] for x in names])
+        cnt, nb = C.c_int(), C.c_size_t()
+        idx, off = (C.c_int * max(1, n))(), (C.c_size_t * max(1, n))()
+        assert L.mpk_chain_saved_layout(ops, n, B, H, W, Cc, C.byref(cnt), idx, off, C.byref(nb)) == 0
+        return [idx[i] for i in range(cnt.value)], [off[i] for i in range(cnt.value)], nb.value
+
+    assert layout(["rotate", "gaussian", "adjust_gamma", "rgb2grey"]) == ([1], [0], 2 * 5 * 4 * 3 * 4)
+    assert layout(["gaussian", "rotate", "brightness"]) == ([1], [0], 2 * 5 * 4 * 3 * 4)
+    # the grey prologue joins the gaussian; the intermediate has one channel
+    assert layout(["rgb2grey", "gaussian", "rotate", "adjust_gamma"]) == ([2], [0], 2 * 5 * 4 * 1 * 4)
+    # transpose and fliplr share a segment; the rotate opens the next
+    assert layout(["transpose", "fliplr", "rotate"]) == ([2], [0], 2 * 4 * 5 * 3 * 4)
+    assert layout(["rotate", "gaussian", "rotate"]) == ([1, 2], [0, 480], 960)
+    assert layout(["brightness", "adjust_gamma"]) == ([], [], 0)
+    assert layout([]) == ([], [], 0)

@@ -235,3 +235,64 @@ def test_channels_first_input(gpu):
     assert y.shape == (2, 32, 40)
     y.sum().backward()
     assert x.grad.shape == x.shape and torch.isfinite(x.grad).all()
+
+
+@pytest.mark.parametrize("chain", [
+    [("rotate", (-30, 30)), ("gaussian", (1.0, 3.0)), ("adjust_gamma", (0.7, 1.5)), ("rgb2grey", None)],
+    [("gaussian", (2.0, 2.0)), ("rotate", (-45, 45)), ("brightness", (-0.1, 0.1))],
+    [("rgb2grey", None), ("gaussian", (0.8, 1.6)), ("transpose", None), ("rotate", (-20, 20)),
+     ("brightness", (-0.2, 0.2)), ("fliplr", None)],
+    [("rotate", (5, 15)), ("rotate", (-40, -10)), ("gaussian", (0.5, 2.5)), ("adjust_gamma", (0.6, 1.4))],
+])
+def test_saved_intermediates_match_recompute(gpu, chain):
+    """The backward reading the forward's saved intermediates gives the
+    gradients of the backward that recomputes every intermediate."""
+    import ctypes as C
+    from millipyde_gb300 import _abi
+    L = _abi.lib()
+    codes = {"rotate": _abi.OP_ROTATE, "gaussian": _abi.OP_GAUSSIAN, "adjust_gamma": _abi.OP_ADJUST_GAMMA,
+             "rgb2grey": _abi.OP_RGB2GREY, "brightness": _abi.OP_BRIGHTNESS, "transpose": _abi.OP_TRANSPOSE,
+             "fliplr": _abi.OP_FLIPLR}
+    rng = np.random.default_rng(len(chain))
+    B, H, W, Cc = 5, 72, 88, 3
+    nops = len(chain)
+    ops = (C.c_int * nops)(*[codes[n] for n, _ in chain])
+    P = np.zeros((B, nops, 3), np.float64)
+    for k, (n, rg) in enumerate(chain):
+        if rg is not None:
+            P[:, k, 0] = rng.uniform(rg[0], rg[1], B)
+        if n == "adjust_gamma":
+            P[:, k, 1] = 1.0
+    ho, wo, co = C.c_int(), C.c_int(), C.c_int()
+    _abi.check(L.mpk_chain_shape(ops, nops, H, W, Cc, C.byref(ho), C.byref(wo), C.byref(co)))
+    x = torch.rand(B, H, W, Cc, device="cuda")
+    y = torch.empty(B, ho.value, wo.value, co.value, device="cuda")
+    gy = torch.randn_like(y)
+    cnt, nbytes = C.c_int(), C.c_size_t()
+    idx, off = (C.c_int * nops)(), (C.c_size_t * nops)()
+    _abi.check(L.mpk_chain_saved_layout(ops, nops, B, H, W, Cc, C.byref(cnt), idx, off, C.byref(nbytes)))
+    assert cnt.value >= 1 and nbytes.value > 0
+    saved = torch.full((nbytes.value // 4,), float("nan"), device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    pp = P.ctypes.data
+    _abi.check(L.mpk_chain_forward_saved(ops, nops, pp, x.data_ptr(), y.data_ptr(), saved.data_ptr(),
+                                         B, H, W, Cc, stream))
+    mask = (C.c_int * nops)(*([1] * nops))
+    res = []
+    for use_saved in (True, False):
+        dx = torch.empty_like(x)
+        dP = torch.zeros(B, nops, 3, dtype=torch.float64, device="cuda")
+        _abi.check(L.mpk_chain_backward_saved(ops, nops, pp, x.data_ptr(),
+                                              saved.data_ptr() if use_saved else None, gy.data_ptr(),
+                                              dx.data_ptr(), dP.data_ptr(), mask, B, H, W, Cc, stream))
+        torch.cuda.synchronize()
+        res.append((dx, dP))
+    (dx1, dp1), (dx0, dp0) = res
+    assert not torch.isnan(saved).any()          # every saved intermediate was written
+    assert rel(dx1, dx0) <= 1e-5
+    assert rel(dp1, dp0) <= 1e-5
+    # and the forward with a saved block writes the same output as without
+    y0 = torch.empty_like(y)
+    _abi.check(L.mpk_chain_forward(ops, nops, pp, x.data_ptr(), y0.data_ptr(), B, H, W, Cc, stream))
+    torch.cuda.synchronize()
+    assert float((y0 - y).abs().max()) <= TOL
