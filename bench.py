@@ -514,8 +514,8 @@ def bench_uniform(args, torch, L, uuid):
 def bench_grad(args, torch, L, uuid, which):
     """grad4: 64 x 512x512x3, rotate U(-30,30) -> gaussian U(1,3) -> gamma
     U(0.7,1.5) -> rgb2grey, loss sum(out*W).  grad5: 16 x 8192x8192x3,
-    gaussian 8 -> rotate U(-45,45) -> brightness U(-0.1,0.1); the backward
-    recomputes the forward."""
+    gaussian 8 -> rotate U(-45,45) -> brightness U(-0.1,0.1); the forward
+    keeps its segment-boundary intermediates for the backward."""
     from millipyde_gb300.autograd import pipeline
     from oracle import oracle as O
     dev = torch.device("cuda:0")
@@ -536,7 +536,8 @@ def bench_grad(args, torch, L, uuid, which):
         ops = [("gaussian", 8.0), ("rotate", theta), ("brightness", delta)]
         params = [theta, delta]
         bpp, wshape = 60, (B, Hh, Ww, 3)
-        desc = "16 x 8192x8192x3, gaussian 8 -> rotate U(-45,45) -> brightness U(-0.1,0.1), recompute"
+        desc = ("16 x 8192x8192x3, gaussian 8 -> rotate U(-45,45) -> brightness U(-0.1,0.1); the backward "
+                "reads the forward's saved blur and back-propagates the brightness from the output")
     x = torch.rand(B, Hh, Ww, 3, device=dev, requires_grad=True)
     Wt = torch.randn(wshape, device=dev)
 

@@ -417,9 +417,14 @@ MPStatus mpk_chain_saved_layout(const int *ops, int nops, int B, int H, int W, i
                                 int *op_index, size_t *offset, size_t *bytes);
 MPStatus mpk_chain_forward_saved(const int *ops, int nops, const double *params, const float *x, float *y,
                                  void *saved, int B, int H, int W, int C, void *stream);
+/* y (may be null) is the forward's output, unmodified: a chain that ends
+ * in a lone brightness back-propagates it from y (clamp01(a + delta) lies
+ * strictly inside (0, 1) exactly when a + delta does), so its input is
+ * neither saved nor recomputed. */
 MPStatus mpk_chain_backward_saved(const int *ops, int nops, const double *params, const float *x,
-                                  const void *saved, const float *dy, float *dx, double *dparams,
-                                  const int *param_mask, int B, int H, int W, int C, void *stream);
+                                  const void *saved, const float *y, const float *dy, float *dx,
+                                  double *dparams, const int *param_mask, int B, int H, int W, int C,
+                                  void *stream);
 
 /* Allocation-free batch.  No counterpart in the reference.  For callers that
  * cannot allocate device memory (GPU memory owned by another allocator or

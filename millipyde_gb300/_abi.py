@@ -150,8 +150,8 @@ SIGNATURES = {
                                      C.POINTER(C.c_size_t)]),
     "mpk_chain_forward_saved": (_ST, [C.POINTER(C.c_int), C.c_int, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int,
                                       C.c_int, _P]),
-    "mpk_chain_backward_saved": (_ST, [C.POINTER(C.c_int), C.c_int, _P, _P, _P, _P, _P, _P, C.POINTER(C.c_int),
-                                       C.c_int, C.c_int, C.c_int, C.c_int, _P]),
+    "mpk_chain_backward_saved": (_ST, [C.POINTER(C.c_int), C.c_int, _P, _P, _P, _P, _P, _P, _P,
+                                       C.POINTER(C.c_int), C.c_int, C.c_int, C.c_int, C.c_int, _P]),
     "mpk_pipeline_run_noalloc": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(MPImage),
                                        C.POINTER(MPImage), C.c_int, C.c_uint64, C.c_uint64, _P]),
     "mpk_pipeline_run_objects": (_ST, [C.POINTER(MPStage), C.c_int, C.POINTER(C.POINTER(MPObjData)),

@@ -37,6 +37,8 @@ _OPS = {
     "colorize": (_abi.OP_COLORIZE, 3),
 }
 _DEFAULTS = {"adjust_gamma": (None, 1.0)}
+# pointwise op codes (a run of them is one adjoint pass)
+_PW = (_abi.OP_RGB2GREY, _abi.OP_BRIGHTNESS, _abi.OP_ADJUST_GAMMA, _abi.OP_COLORIZE)
 
 _L = None
 
@@ -137,14 +139,20 @@ class _ChainFn(torch.autograd.Function):
                                              saved.data_ptr() if saved is not None else None,
                                              B, H, W, Cc, stream))
         ctx.saved_inter = saved
-        ctx.save_for_backward(x)
+        # a chain ending in a lone brightness back-propagates it from y
+        ctx.y_used = nops >= 1 and names[-1] == "brightness" and (nops == 1 or _OPS[names[-2]][0] not in _PW)
+        if ctx.y_used:
+            ctx.save_for_backward(x, y)
+        else:
+            ctx.save_for_backward(x)
         ctx.P, ctx.names, ctx.slots, ctx.nparams = P, names, slots, len(ptensors)
         ctx.pshapes = [(t.shape, t.dtype, t.device) for t in ptensors]
         return y
 
     @staticmethod
     def backward(ctx, gy):
-        (x,) = ctx.saved_tensors
+        x = ctx.saved_tensors[0]
+        y = ctx.saved_tensors[1] if ctx.y_used else None
         B, H, W, Cc = x.shape
         gy = gy.contiguous()
         dx = torch.empty_like(x)
@@ -160,6 +168,7 @@ class _ChainFn(torch.autograd.Function):
         sv = ctx.saved_inter
         _abi.check(L.mpk_chain_backward_saved(_opcodes(ctx.names), nops, ctx.P.data_ptr(), x.data_ptr(),
                                               sv.data_ptr() if sv is not None else None,
+                                              y.data_ptr() if y is not None else None,
                                               gy.data_ptr(), dx.data_ptr(), dP.data_ptr(), mask,
                                               B, H, W, Cc, stream))
         ctx.saved_inter = None

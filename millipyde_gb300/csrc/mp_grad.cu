@@ -5,6 +5,8 @@
 //               run in registers from its input x, back-propagates the
 //               output gradient g through the run in reverse and accumulates
 //               the parameter gradients (d delta, d gamma, d gain, d mult).
+//               A chain's final lone brightness runs from the chain's output
+//               instead (MP_OP_BRIGHTNESS_OUT), so its input is not needed.
 //   ROTATE_ADJ  dx = R^T g, the exact transpose of the forward bilinear
 //               gather: for each source pixel q the kernel visits the (at most
 //               4x4) output pixels p whose forward sample used q, recomputes
@@ -65,6 +67,17 @@ __device__ __forceinline__ void mp_pw_back(const PwOp &o, const float v[4], int 
             if (k < cc) {
                 const float t = v[k] + o.p0;
                 const float m = (t > 0.0f && t < 1.0f) ? g[k] : 0.0f;
+                gi[k] = m;
+                pa[0] += m;
+            }
+        }
+        break;
+    case MP_OP_BRIGHTNESS_OUT:
+        // v is the op's output: inside (0, 1) iff the clamp was not active
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            if (k < cc) {
+                const float m = (v[k] > 0.0f && v[k] < 1.0f) ? g[k] : 0.0f;
                 gi[k] = m;
                 pa[0] += m;
             }
@@ -170,7 +183,7 @@ __device__ void mp_point_adj_tile(const MPJob &J, int t, float *red)
     }
     if (!J.acc) return;
     for (int k = 0; k < n; ++k) {
-        const int np = (J.pro.op[k].op == MP_OP_BRIGHTNESS) ? 1
+        const int np = (J.pro.op[k].op == MP_OP_BRIGHTNESS || J.pro.op[k].op == MP_OP_BRIGHTNESS_OUT) ? 1
                      : (J.pro.op[k].op == MP_OP_ADJUST_GAMMA) ? 2
                      : (J.pro.op[k].op == MP_OP_COLORIZE) ? 3 : 0;
         for (int j = 0; j < np; ++j) {

@@ -15,6 +15,10 @@
 // Limits
 // ---------------------------------------------------------------------------
 #define MP_MAX_PW 8                       // pointwise ops in one prologue/epilogue
+// Internal op of the pointwise adjoint: brightness back-propagated from its
+// OUTPUT v = clamp01(x + delta).  v lies strictly inside (0, 1) exactly when
+// x + delta does, so the gradient mask (and d delta) needs no x.
+#define MP_OP_BRIGHTNESS_OUT 64
 #define MP_MAX_TAPS (2 * MP_MAX_RADIUS + 1)
 #define MP_FIX_FRAC 40                    // fractional bits of rotate coordinates
 #define MP_SPIN_FAST 2048                 // try_wait polls before backing off

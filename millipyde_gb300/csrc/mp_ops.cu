@@ -2245,13 +2245,14 @@ extern "C" MPStatus mpk_chain_backward_masked(const int *ops, int nops, const do
                                               const float *dy, float *dx, double *dparams, const int *param_mask,
                                               int B, int H, int W, int C, void *stream)
 {
-    return mpk_chain_backward_saved(ops, nops, params, x, nullptr, dy, dx, dparams, param_mask, B, H, W, C,
-                                    stream);
+    return mpk_chain_backward_saved(ops, nops, params, x, nullptr, nullptr, dy, dx, dparams, param_mask, B, H, W,
+                                    C, stream);
 }
 
 extern "C" MPStatus mpk_chain_backward_saved(const int *ops, int nops, const double *params, const float *x,
-                                             const void *saved, const float *dy, float *dx, double *dparams,
-                                             const int *param_mask, int B, int H, int W, int C, void *stream)
+                                             const void *saved, const float *y, const float *dy, float *dx,
+                                             double *dparams, const int *param_mask, int B, int H, int W, int C,
+                                             void *stream)
 {
     // param_mask[k] != 0: the parameters of op k want a gradient (null: all ops)
     auto wants = [&](int k) { return dparams && (!param_mask || param_mask[k] != 0); };
@@ -2288,13 +2289,17 @@ extern "C" MPStatus mpk_chain_backward_saved(const int *ops, int nops, const dou
     // wants a gradient (the d sigma dot passes) and of every rotate (d theta,
     // and the gather adjoint's source geometry); transpose and fliplr read
     // none.
+    // A final lone brightness back-propagates from the chain's output y
+    // (when given) and reads no intermediate.
+    const bool tail_from_y = y && nops >= 1 && ops[nops - 1] == MP_OP_BRIGHTNESS &&
+                             (nops == 1 || !mp_is_pointwise(ops[nops - 2]));
     std::vector<char> need(nops + 1, 0);
     for (int k = nops - 1; k >= 0;) {
         int j = k;
         if (mp_is_pointwise(ops[k]))
             while (j > 0 && mp_is_pointwise(ops[j - 1]) && k - (j - 1) < MP_MAX_PW) --j;
-        const bool reads = mp_is_pointwise(ops[k]) || ops[k] == MP_OP_ROTATE ||
-                           (ops[k] == MP_OP_GAUSSIAN && wants(k));
+        const bool reads = (mp_is_pointwise(ops[k]) && !(tail_from_y && k == nops - 1)) ||
+                           ops[k] == MP_OP_ROTATE || (ops[k] == MP_OP_GAUSSIAN && wants(k));
         if (reads) need[j] = 1;
         k = j - 1;
     }
@@ -2439,9 +2444,13 @@ extern "C" MPStatus mpk_chain_backward_saved(const int *ops, int nops, const dou
                         ROp r = mp_rop(ops[t], params + ((size_t)(b0 + q) * nops + t) * 3);
                         mp_pw_push(sg.pro, r);
                     }
-                    const MPImage a = a_img(q, j), go = gout_img(q), gi = gin_img(q);
+                    // the final lone brightness reads the chain's output
+                    const bool from_y = tail_from_y && k == nops - 1 && j == k;
+                    const MPImage a = from_y ? mp_dense_image(y, b0 + q, sh[nops]) : a_img(q, j);
+                    const MPImage go = gout_img(q), gi = gin_img(q);
                     st = mp_fill_job(J, sg, a, gi, 0, 0);
                     if (st != MILLIPYDE_SUCCESS) break;
+                    if (from_y) J.pro.op[0].op = MP_OP_BRIGHTNESS_OUT;
                     J.cin = sh[j].c;
                     J.aux = (const float *)go.data;
                     J.aux_pitch = go.pitch / 4;

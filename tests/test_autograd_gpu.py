@@ -243,10 +243,13 @@ def test_channels_first_input(gpu):
     [("rgb2grey", None), ("gaussian", (0.8, 1.6)), ("transpose", None), ("rotate", (-20, 20)),
      ("brightness", (-0.2, 0.2)), ("fliplr", None)],
     [("rotate", (5, 15)), ("rotate", (-40, -10)), ("gaussian", (0.5, 2.5)), ("adjust_gamma", (0.6, 1.4))],
+    [("rotate", (-30, 30)), ("adjust_gamma", (0.6, 1.4)), ("brightness", (-0.3, 0.3))],
+    [("transpose", None), ("gaussian", (1.0, 2.0)), ("brightness", (-0.4, 0.4))],
 ])
 def test_saved_intermediates_match_recompute(gpu, chain):
-    """The backward reading the forward's saved intermediates gives the
-    gradients of the backward that recomputes every intermediate."""
+    """The backward reading the forward's saved intermediates (and, for a
+    final lone brightness, the output) gives the gradients of the backward
+    that recomputes every intermediate."""
     import ctypes as C
     from millipyde_gb300 import _abi
     L = _abi.lib()
@@ -271,24 +274,28 @@ def test_saved_intermediates_match_recompute(gpu, chain):
     cnt, nbytes = C.c_int(), C.c_size_t()
     idx, off = (C.c_int * nops)(), (C.c_size_t * nops)()
     _abi.check(L.mpk_chain_saved_layout(ops, nops, B, H, W, Cc, C.byref(cnt), idx, off, C.byref(nbytes)))
-    assert cnt.value >= 1 and nbytes.value > 0
-    saved = torch.full((nbytes.value // 4,), float("nan"), device="cuda")
+    assert (cnt.value == 0) == (nbytes.value == 0)
+    saved = torch.full((max(1, nbytes.value // 4),), float("nan"), device="cuda")
+    sp = saved.data_ptr() if nbytes.value else None
     stream = torch.cuda.current_stream().cuda_stream
     pp = P.ctypes.data
-    _abi.check(L.mpk_chain_forward_saved(ops, nops, pp, x.data_ptr(), y.data_ptr(), saved.data_ptr(),
-                                         B, H, W, Cc, stream))
+    _abi.check(L.mpk_chain_forward_saved(ops, nops, pp, x.data_ptr(), y.data_ptr(), sp, B, H, W, Cc, stream))
     mask = (C.c_int * nops)(*([1] * nops))
     res = []
     for use_saved in (True, False):
         dx = torch.empty_like(x)
         dP = torch.zeros(B, nops, 3, dtype=torch.float64, device="cuda")
+        # the saved variant also hands over y (a final lone brightness
+        # back-propagates from it); the reference recomputes everything
         _abi.check(L.mpk_chain_backward_saved(ops, nops, pp, x.data_ptr(),
-                                              saved.data_ptr() if use_saved else None, gy.data_ptr(),
+                                              sp if use_saved else None,
+                                              y.data_ptr() if use_saved else None, gy.data_ptr(),
                                               dx.data_ptr(), dP.data_ptr(), mask, B, H, W, Cc, stream))
         torch.cuda.synchronize()
         res.append((dx, dP))
     (dx1, dp1), (dx0, dp0) = res
-    assert not torch.isnan(saved).any()          # every saved intermediate was written
+    if nbytes.value:
+        assert not torch.isnan(saved).any()      # every saved intermediate was written
     assert rel(dx1, dx0) <= 1e-5
     assert rel(dp1, dp0) <= 1e-5
     # and the forward with a saved block writes the same output as without
