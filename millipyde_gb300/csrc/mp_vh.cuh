@@ -46,6 +46,12 @@
 #ifndef MP_VH_PAIR_RMAX
 #define MP_VH_PAIR_RMAX 4
 #endif
+// Row pairing in the radius-bucket kernels (256 threads, 1 CTA per SM):
+// measured slower (8192x8192 RGB, radius 24: 97.7 against 87.5 ms for a
+// training step with two such blurs per image), so off.
+#ifndef MP_VH_PAIR_BIG
+#define MP_VH_PAIR_BIG 0
+#endif
 
 namespace mp_vh {
 
@@ -153,7 +159,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     // the plain one-channel family computes two output rows per
     // horizontal work item as packed pairs, and so does the channel-
     // preserving family up to radius MP_VH_PAIR_RMAX
-    constexpr bool PAIR = (CM == 1 || R <= MP_VH_PAIR_RMAX) && !BIG && !DOT;
+    constexpr bool PAIR = (BIG ? MP_VH_PAIR_BIG != 0 : (CM == 1 || R <= MP_VH_PAIR_RMAX)) && !DOT;
     constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
     constexpr int D = R8 - R;                             // tap offset inside the window
     constexpr int NWIN = VR + 2 * R8;
