@@ -521,22 +521,22 @@ def bench_grad(args, torch, L, uuid, which):
     dev = torch.device("cuda:0")
     torch.manual_seed(SEED)
     if which == "grad4":
-        B, Hh, Ww = 64, 512, 512
+        B, Hh, Ww = (args.images if args.workload == which and args.images else 64), 512, 512
         theta = (torch.rand(B, dtype=torch.float64, device=dev) * 60 - 30).requires_grad_()
         sigma = (1 + 2 * torch.rand(B, dtype=torch.float64, device=dev)).requires_grad_()
         gamma = (0.7 + 0.8 * torch.rand(B, dtype=torch.float64, device=dev)).requires_grad_()
         ops = [("rotate", theta), ("gaussian", sigma), ("adjust_gamma", gamma), ("rgb2grey",)]
         params = [theta, sigma, gamma]
         bpp, wshape = 44, (B, Hh, Ww)
-        desc = "64 x 512x512x3, rotate U(-30,30) -> gaussian U(1,3) -> gamma U(0.7,1.5) -> rgb2grey"
+        desc = "%d x 512x512x3, rotate U(-30,30) -> gaussian U(1,3) -> gamma U(0.7,1.5) -> rgb2grey" % B
     else:
-        B, Hh, Ww = 16, 8192, 8192
+        B, Hh, Ww = (args.images if args.workload == which and args.images else 16), 8192, 8192
         theta = (torch.rand(B, dtype=torch.float64, device=dev) * 90 - 45).requires_grad_()
         delta = (torch.rand(B, dtype=torch.float64, device=dev) * 0.2 - 0.1).requires_grad_()
         ops = [("gaussian", 8.0), ("rotate", theta), ("brightness", delta)]
         params = [theta, delta]
         bpp, wshape = 60, (B, Hh, Ww, 3)
-        desc = ("16 x 8192x8192x3, gaussian 8 -> rotate U(-45,45) -> brightness U(-0.1,0.1); the backward "
+        desc = ("%d x 8192x8192x3, gaussian 8 -> rotate U(-45,45) -> brightness U(-0.1,0.1); the backward " % B +
                 "reads the forward's saved blur and back-propagates the brightness from the output")
     x = torch.rand(B, Hh, Ww, 3, device=dev, requires_grad=True)
     Wt = torch.randn(wshape, device=dev)
@@ -802,7 +802,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--images", type=int, default=0,
-                    help="ragged batch size (default 1000; profiling runs use a smaller batch)")
+                    help="batch size of the selected --workload (default: ragged 1000, uniform 256, "
+                         "grad4 64, grad5 16; profiling runs use a smaller batch)")
     ap.add_argument("--legs", default="all", choices=["all", "fused"],
                     help="'fused' times only the fused plan (profiling runs)")
     ap.add_argument("--fuse", default="auto", choices=["auto", "on", "off"],
