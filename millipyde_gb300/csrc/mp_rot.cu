@@ -72,13 +72,23 @@ __device__ __forceinline__ void ro_origin_adj(const MPJob &J, int lt, int TW, in
 }
 
 // Per-buffer tile record written by the issuing thread: footprint origin
-// (pixels) and output tile origin.
+// (pixels), output tile origin, and the job fields the tile's threads use.
+// The job table lives in global memory and the footprint buffers leave
+// little L1 beside them, so reading the fields there cost each tile an L2
+// round trip; the issuing thread copies them here one tile ahead.
 struct RoTile {
     int bx, by, x0, y0;
+    int jidx;                  // job of the tile (batch launches)
+    int w, h, wo, ho, bxw, dp, flip;
+    int en, eop;               // epilogue length and first op
+    float e0, e1, e2;          // first op's parameters
+    long long cq, sq;
+    float *dst;
 };
+static_assert(sizeof(RoTile) <= 112, "two tile records must fit below the footprint buffers");
 
 template <int C, int MODE = RO_FWD>
-__device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uint64_t *bar, RoTile *rec)
+__device__ __forceinline__ void ro_issue(const MPJob &J, int jidx, int lt, float *buf, uint64_t *bar, RoTile *rec)
 {
     int bx, by, x0, y0;
     if (MODE == RO_ADJ) ro_origin_adj(J, lt, mp_ro_tw(C), mp_ro_th(C), &bx, &by, &x0, &y0);
@@ -87,6 +97,22 @@ __device__ __forceinline__ void ro_issue(const MPJob &J, int lt, float *buf, uin
     rec->by = by;
     rec->x0 = x0;
     rec->y0 = y0;
+    rec->jidx = jidx;
+    rec->w = J.w;
+    rec->h = J.h;
+    rec->wo = J.wo;
+    rec->ho = J.ho;
+    rec->bxw = J.bxw;
+    rec->dp = J.dst_pitch;
+    rec->flip = J.flip;
+    rec->en = J.epi.n;
+    rec->eop = J.epi.n ? J.epi.op[0].op : 0;
+    rec->e0 = J.epi.op[0].p0;
+    rec->e1 = J.epi.op[0].p1;
+    rec->e2 = J.epi.op[0].p2;
+    rec->cq = J.cosq;
+    rec->sq = J.sinq;
+    rec->dst = J.dst;
     const int xf = bx * C;
     mp_mbar_arrive_expect_tx(bar, (uint32_t)(J.bxw * J.byh * 4));
     mp_tma_load_2d(buf, &J.tmap, bar, xf & ~3, by);
@@ -130,12 +156,12 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
     constexpr int RSTEP = NT / TW, NPX = TW * TH / NT;
     const int bx = T.bx, by = T.by, x0 = T.x0, y0 = T.y0;
     const int delta = bx * C - ((bx * C) & ~3);
-    const int bxw = J.bxw;
+    const int bxw = T.bxw;
     const int x = x0 + (threadIdx.x & (TW - 1));
     const int yf = y0 + threadIdx.x / TW;
-    const int wo = J.wo, ho = J.ho;
+    const int wo = T.wo, ho = T.ho;
     if (x >= wo) return;
-    const long long W = J.w, H = J.h, cq = J.cosq, sq = J.sinq;
+    const long long W = T.w, H = T.h, cq = T.cq, sq = T.sq;
     const long long X2 = 2LL * x - W, Y2 = 2LL * yf - H;
     // sample position relative to the box origin: exact in MP_FIX_FRAC fixed
     // point for the thread's first pixel, then stepped in 8.24 fixed point
@@ -146,11 +172,10 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
     int lx = (int)(rx0 >> (MP_FIX_FRAC - 24)), ly = (int)(ry0 >> (MP_FIX_FRAC - 24));
     const int stx = (int)((-2LL * RSTEP * sq) >> (MP_FIX_FRAC - 24));
     const int sty = (int)((2LL * RSTEP * cq) >> (MP_FIX_FRAC - 24));
-    const PwFast epi = mp_pw_fast(J.epi);
-    const float e0 = epi.p0, e1 = epi.p1;
-    const int dp = J.dst_pitch;
-    const int xo = J.flip ? (wo - 1 - x) : x;
-    float *drow = J.dst + (size_t)yf * dp + (size_t)xo * C;
+    const float e0 = T.e0, e1 = T.e1, e2 = T.e2;
+    const int dp = T.dp;
+    const int xo = T.flip ? (wo - 1 - x) : x;
+    float *drow = T.dst + (size_t)yf * dp + (size_t)xo * C;
     const size_t rstride = (size_t)RSTEP * dp;
     const bool full = y0 + TH <= ho;
     if constexpr (C == 1 && (EK == RO_EPI_NONE || EK == RO_EPI_GAMMA || EK == RO_EPI_BRIGHT)) {
@@ -202,8 +227,8 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
                 v[k] = gy * (gx * p0[k] + fx * p0[C + k]) + fy * (gx * p1[k] + fx * p1[C + k]);
             if (EK == RO_EPI_LIST) {
                 // general list: the output may have fewer channels
-                const int c2 = mp_pw_apply_f(epi, J.epi, v, C);
-                float *d = J.dst + (size_t)(yf + RSTEP * i) * dp + (size_t)xo * c2;
+                const int c2 = mp_pw_apply(J.epi, v, C);
+                float *d = T.dst + (size_t)(yf + RSTEP * i) * dp + (size_t)xo * c2;
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
                     if (k < c2) d[k] = v[k];
@@ -214,7 +239,7 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
                     float o = v[k];
                     if (EK == RO_EPI_GAMMA && colour) o = mp_clamp01(e1 * __powf(o, e0));
                     else if (EK == RO_EPI_BRIGHT && colour) o = mp_clamp01(o + e0);
-                    else if (EK == RO_EPI_ONE) o = mp_pw_chan(epi.op, epi.p0, epi.p1, epi.p2, o, k, C);
+                    else if (EK == RO_EPI_ONE) o = mp_pw_chan(T.eop, e0, e1, e2, o, k, C);
                     drow[k] = o;
                 }
             }
@@ -228,8 +253,8 @@ __device__ __forceinline__ void ro_tile_k(const MPJob &J, const RoTile &T, const
 template <int C>
 __device__ __forceinline__ void ro_tile(const MPJob &J, const RoTile &T, const float *buf)
 {
-    const int n = J.epi.n;
-    const int op = J.epi.op[0].op;
+    const int n = T.en;
+    const int op = T.eop;
     if (n == 0) ro_tile_k<C, RO_EPI_NONE>(J, T, buf);
     else if (n == 1 && op == MP_OP_ADJUST_GAMMA) ro_tile_k<C, RO_EPI_GAMMA>(J, T, buf);
     else if (n == 1 && op == MP_OP_BRIGHTNESS) ro_tile_k<C, RO_EPI_BRIGHT>(J, T, buf);
@@ -410,7 +435,7 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
     unsigned char *base = ro_base(mp_ro_smem);
     uint64_t *bars = reinterpret_cast<uint64_t *>(base);
     RoTile *recs = reinterpret_cast<RoTile *>(base + 16);   // one record per buffer
-    float *bufs = reinterpret_cast<float *>(base + 128);
+    float *bufs = reinterpret_cast<float *>(base + 256);
     if (threadIdx.x == 0) {
         mp_mbar_init(bars, 1);
         mp_mbar_init(bars + 1, 1);
@@ -418,19 +443,18 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
     }
     __syncthreads();
     const int first = blockIdx.x, step = gridDim.x;
-    auto job_of = [&](int t) -> const MPJob & { return one ? *one : jobs[__ldg(tile_job + t)]; };
     if (threadIdx.x == 0) {
         for (int k = 0; k < 2; ++k) {
             const int t = first + k * step;
             if (t >= total) break;
-            const MPJob &J = job_of(t);
+            const int ji = one ? 0 : __ldg(tile_job + t);
+            const MPJob &J = one ? *one : jobs[ji];
             if (!one) mp_tensormap_acquire(&J.tmap);
-            ro_issue<C, MODE>(J, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k, recs + k);
+            ro_issue<C, MODE>(J, ji, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k, recs + k);
         }
     }
     int k = 0;
     for (int t = first; t < total; t += step, ++k) {
-        const MPJob &J = job_of(t);
         const float *buf = bufs + (k & 1) * buf_floats;
         const bool ok = mp_mbar_wait_bounded(bars + (k & 1), (uint32_t)(k >> 1) & 1u);
         if (!__syncthreads_and(ok)) {
@@ -440,6 +464,7 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
             return;
         }
         const RoTile rec = recs[k & 1];
+        const MPJob &J = one ? *one : jobs[rec.jidx];
         if (MODE == RO_FWD) {
             ro_tile<C>(J, rec, buf);
         } else if (MODE == RO_ADJ) {
@@ -460,9 +485,10 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
         if (threadIdx.x == 0) {
             const int tn = t + 2 * step;
             if (tn < total) {
-                const MPJob &Jn = job_of(tn);
+                const int jn = one ? 0 : __ldg(tile_job + tn);
+                const MPJob &Jn = one ? *one : jobs[jn];
                 if (!one) mp_tensormap_acquire(&Jn.tmap);
-                ro_issue<C, MODE>(Jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1),
+                ro_issue<C, MODE>(Jn, jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1),
                                   recs + (k & 1));
             }
         }
@@ -526,7 +552,7 @@ static const void *mp_ro_fn(int c, bool single)
     }
 }
 
-size_t mp_ro_smem(int buf_floats) { return 128 + 2 * (size_t)buf_floats * 4 + 128; }
+size_t mp_ro_smem(int buf_floats) { return 256 + 2 * (size_t)buf_floats * 4 + 128; }
 
 MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
 {
