@@ -283,3 +283,42 @@ def test_plan_capture_in_fresh_process(gpu):
                        timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.startswith("ok")
+
+
+def _launch_kinds(spec_stages, nst, xs):
+    L = _abi.lib()
+    keep, ins = [], []
+    for x in xs:
+        t, m = dev_image(x)
+        keep.append(t)
+        ins.append(m)
+    ia = _abi.images(ins)
+    outs = _abi.images([_abi.MPImage() for _ in xs])
+    _abi.check(L.mpk_pipeline_shapes(spec_stages, nst, ia, outs, len(xs), 0, 0))
+    keep += [alloc_like(outs[i]) for i in range(len(xs))]
+    plan = C.c_void_p()
+    _abi.check(L.mpk_plan_create(spec_stages, nst, ia, outs, len(xs), 0, 0, None, C.byref(plan)))
+    kinds = []
+    for i in range(L.mpk_plan_num_launches(plan)):
+        k = C.c_int()
+        L.mpk_plan_launch_info(plan, i, C.byref(k), None, None, None)
+        kinds.append(k.value)
+    _abi.check(L.mpk_plan_destroy(plan))
+    torch.cuda.synchronize()
+    return kinds
+
+
+@pytest.mark.parametrize("sigma", [1.3, 3.0, 6.0])
+def test_grey_after_colour_gaussian_is_split(gpu, rng, sigma):
+    """rgb2grey after a colour gaussian (no spatial op after it) runs as a
+    pointwise pass after the channel-preserving streaming blur; with a
+    rotate after it the grey stays the blur's epilogue."""
+    xs = [rng.random((h, w, 3), dtype=np.float32) for h, w in ((96, 128), (61, 203), (300, 40))]
+    spec = [dict(op="gaussian", lo=(sigma,)), dict(op="adjust_gamma", lo=(0.7, 1.0)), dict(op="rgb2grey"),
+            dict(op="brightness", lo=(0.05,))]
+    check_spec(spec, xs)
+    kinds = _launch_kinds(_abi.stages(*[to_stage(d) for d in spec]), len(spec), xs)
+    assert kinds[-1] == 0                       # MPK_POINT last: the grey split off the blur
+    spec2 = [dict(op="gaussian", lo=(sigma,)), dict(op="rgb2grey"), dict(op="rotate", lo=(12.0,))]
+    check_spec(spec2, xs)
+    assert 0 not in _launch_kinds(_abi.stages(*[to_stage(d) for d in spec2]), len(spec2), xs)
