@@ -594,32 +594,6 @@ static bool mp_rot_setup(int c, int buf_floats, int *grid)
     return true;
 }
 
-// Largest footprint buffer (floats, a multiple of 32) that keeps the
-// resident CTAs per SM of a launch whose largest box needs `buf_floats`:
-// the room that bank-conflict padding may use for free.
-static int mp_rot_buf_cap(int c, int buf_floats)
-{
-    int cps0 = 0;
-    if (mp_ro_prepare(c, mp_ro_smem(buf_floats), &cps0) != MILLIPYDE_SUCCESS) {
-        cudaGetLastError();
-        return buf_floats;
-    }
-    int lo = buf_floats, hi = buf_floats + 8192;
-    while (hi - lo > 32) {
-        const int mid = ((lo + hi) / 2) & ~31;
-        const size_t smem = mp_ro_smem(mid);
-        int cps = 0;
-        bool keep = false;
-        if (mid > lo && smem <= (size_t)mp_max_smem_optin()) {
-            if (mp_ro_prepare(c, smem, &cps) == MILLIPYDE_SUCCESS) keep = cps >= cps0;
-            else cudaGetLastError();
-        }
-        if (keep) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
 static void mp_seg_tiles(const Seg &sg, int *tw, int *th)
 {
     *tw = *th = 0;
@@ -885,17 +859,14 @@ static MPStatus mp_add_rot(MPTables &T, std::vector<MPLaunch> &launches, const s
         bytes += 4.0 * ((double)srcs[i].height * srcs[i].width * srcs[i].channels +
                         (double)dsts[i].height * dsts[i].width * dsts[i].channels);
     }
-    // boxes re-encoded with a bank-friendly pitch where the buffer has room
-    // at the same occupancy
-    const int c0 = sgs[0].cin;
-    const int cap = mp_rot_buf_cap(c0, bufmax);
+    // boxes re-encoded with a bank-friendly pitch where it fits the buffer
     for (size_t i = 0; i < sgs.size(); ++i) {
-        const int p = mp_rot_padded_bxw(js[i], cap);
+        const int p = mp_rot_padded_bxw(js[i], bufmax);
         if (p > js[i].bxw && mp_fill_job_rot(js[i], sgs[i], srcs[i], dsts[i], false, p) != MILLIPYDE_SUCCESS)
             return MILLIPYDE_SUCCESS;
-        bufmax = std::max(bufmax, mp_rot_buf_floats(js[i]));
     }
     int grid = 0;
+    const int c0 = sgs[0].cin;
     if (!mp_rot_setup(c0, bufmax, &grid)) return MILLIPYDE_SUCCESS;
     const size_t nl = launches.size();
     MPStatus st = T.add(launches, MPK_RSTREAM, c0, mp_ro_smem(bufmax), js, bytes);
