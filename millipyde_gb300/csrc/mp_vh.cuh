@@ -49,6 +49,12 @@
 // Row pairing in the radius-bucket kernels (256 threads, 1 CTA per SM):
 // measured slower (8192x8192 RGB, radius 24: 97.7 against 87.5 ms for a
 // training step with two such blurs per image), so off.
+// Horizontal pass of the channel-preserving and bucket kernels with
+// adjacent outputs packed in f32x2 pairs where their operands are an
+// aligned register pair (1 = on).
+#ifndef MP_VH_HPACK
+#define MP_VH_HPACK 1
+#endif
 #ifndef MP_VH_PAIR_BIG
 #define MP_VH_PAIR_BIG 0
 #endif
@@ -485,6 +491,52 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                             else a0 = fmaf(htap(m), x[E + k + m], a0);
                         }
                         o[k] = a0 + a1;
+                    }
+                } else if constexpr (!DOT && MP_VH_HPACK) {
+                    // taps CM floats apart: consume the tile row in order so
+                    // that only the 8 sums stay live.  Outputs 2j and 2j + 1
+                    // use the same tap at positions p and p + 1: where p is
+                    // even the two operands are one aligned register pair of
+                    // the float4 and take one f32x2 FMA, else two scalar
+                    // FMAs (an operand that opens the next float4 is added
+                    // there).  Each output still sums its taps in position
+                    // order.
+                    float2 o2[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) o2[j] = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int q = 0; q < NLD; ++q) {
+                        const float4 v = ld4(gp + 4 * q);
+                        const float e4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            // output 2j + 1 at position 4q, its tap found at 4q - 1 for output 2j
+                            const int t = 4 * q - 1 - E - 2 * j;
+                            if (q > 0 && t >= 0 && t % CM == 0 && t / CM < NTAP)
+                                o2[j].y = fmaf(htap(t / CM), e4[0], o2[j].y);
+                        }
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) {
+                                const int t = 4 * q + u - E - 2 * j;   // = m * CM for tap m of output 2j
+                                if (t >= 0 && t % CM == 0 && t / CM < NTAP) {
+                                    const int m = t / CM;
+                                    if (u % 2 == 0) {
+                                        o2[j] = fma2(w2[BIG ? (m <= R ? m : 2 * R - m) : m],
+                                                     make_float2(e4[u], e4[u + 1]), o2[j]);
+                                    } else {
+                                        o2[j].x = fmaf(htap(m), e4[u], o2[j].x);
+                                        if (u == 1) o2[j].y = fmaf(htap(m), e4[2], o2[j].y);
+                                    }
+                                }
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        o[2 * j] = o2[j].x;
+                        o[2 * j + 1] = o2[j].y;
                     }
                 } else {
                     // taps CM floats apart: consume the tile row in order so
