@@ -47,6 +47,7 @@ enum MPKind {
 __host__ __device__ constexpr int mp_ro_tw(int c) { return c == 1 ? 64 : 32; }
 __host__ __device__ constexpr int mp_ro_th(int c) { return c == 1 ? 64 : 32; }
 #define MP_RO_NT 256
+#define MP_RO_NT_FWD (MP_RO_NT + 32)   // forward rotate: sampling threads + a producer warp
 
 // ---------------------------------------------------------------------------
 // Streaming gaussian geometry (host and device agree on it).  Rows are
@@ -350,6 +351,11 @@ __device__ __forceinline__ void mp_mbar_arrive_expect_tx(uint64_t *bar, uint32_t
                      mp_smem_addr(bar)),
                  "r"(bytes)
                  : "memory");
+}
+
+__device__ __forceinline__ void mp_mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mp_smem_addr(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mp_mbar_try_wait(uint64_t *bar, uint32_t parity)

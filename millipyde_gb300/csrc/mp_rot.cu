@@ -407,6 +407,70 @@ __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
     return smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
 }
 
+// Forward rotate, warp-specialised: MP_RO_NT sampling threads and one
+// producer warp whose lane 0 copies each tile's job fields into its record
+// and issues its footprint's TMA.  Buffer k & 1 holds tile k; `full` says
+// its copy landed, `empty` that every sampling thread is done with it (each
+// arrives after its tile's stores, which consume every value it loaded).
+// No block-wide barrier: sampling warps never wait for the issuing
+// thread's job-table reads or for each other.  Every wait is bounded; after
+// a timeout the producer lets its copies in flight land before it returns.
+template <int C>
+__device__ __forceinline__ void ro_run_fwd(const MPJob *jobs, const int *tile_job, const MPJob *one, int total,
+                                           int buf_floats, int *err)
+{
+    extern __shared__ unsigned char mp_ro_smem[];
+    unsigned char *base = ro_base(mp_ro_smem);
+    uint64_t *full = reinterpret_cast<uint64_t *>(base);          // [2]
+    uint64_t *empty = full + 2;                                    // [2]
+    RoTile *recs = reinterpret_cast<RoTile *>(base + 32);         // one record per buffer
+    float *bufs = reinterpret_cast<float *>(base + 256);
+    if (threadIdx.x == 0) {
+        mp_mbar_init(full, 1);
+        mp_mbar_init(full + 1, 1);
+        mp_mbar_init(empty, MP_RO_NT);
+        mp_mbar_init(empty + 1, MP_RO_NT);
+        mp_fence_barrier_init();
+    }
+    __syncthreads();
+    const int first = blockIdx.x, step = gridDim.x;
+    if (threadIdx.x >= MP_RO_NT) {
+        if (threadIdx.x != MP_RO_NT) return;
+        int k = 0;
+        bool ok = true;
+        for (int t = first; t < total; t += step, ++k) {
+            const int b = k & 1;
+            if (k >= 2 && !mp_mbar_wait_bounded(empty + b, (uint32_t)((k >> 1) - 1) & 1u)) {
+                ok = false;
+                break;
+            }
+            const int ji = one ? 0 : __ldg(tile_job + t);
+            const MPJob &J = one ? *one : jobs[ji];
+            if (!one) mp_tensormap_acquire(&J.tmap);
+            ro_issue<C, RO_FWD>(J, ji, one ? t : t - J.tile0, bufs + b * buf_floats, full + b, recs + b);
+        }
+        if (!ok) {
+            atomicExch(err, MP_KERR_TIMEOUT);
+            // tiles k - 2 and k - 1 were issued last (one per buffer)
+            for (int q = k - 2; q < k; ++q)
+                if (q >= 0) mp_mbar_wait_bounded(full + (q & 1), (uint32_t)(q >> 1) & 1u);
+        }
+        return;
+    }
+    int k = 0;
+    for (int t = first; t < total; t += step, ++k) {
+        const int b = k & 1;
+        if (!mp_mbar_wait_bounded(full + b, (uint32_t)(k >> 1) & 1u)) {
+            atomicExch(err, MP_KERR_TIMEOUT);
+            return;
+        }
+        const RoTile rec = recs[b];
+        const MPJob &J = one ? *one : jobs[rec.jidx];
+        ro_tile<C>(J, rec, bufs + b * buf_floats);
+        mp_mbar_arrive(empty + b);
+    }
+}
+
 // Persistent loop over tiles t = first, first + step, ... of a tile -> job map
 // (or of one job when `jobs` is null).  Buffer k & 1 holds tile k's footprint.
 template <int C, int MODE = RO_FWD>
@@ -499,16 +563,16 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
 }  // namespace
 
 #define MP_RO_KERNELS(NAME, C)                                                                       \
-    __global__ void __launch_bounds__(MP_RO_NT) NAME##_batch(const MPJob *__restrict__ jobs,        \
-                                                             const int *__restrict__ tile_job,      \
-                                                             int total, int buf_floats, int *err)   \
+    __global__ void __launch_bounds__(MP_RO_NT_FWD) NAME##_batch(const MPJob *__restrict__ jobs,    \
+                                                                 const int *__restrict__ tile_job,  \
+                                                                 int total, int buf_floats, int *err) \
     {                                                                                               \
-        ro_run<C>(jobs, tile_job, nullptr, total, buf_floats, err);                                  \
+        ro_run_fwd<C>(jobs, tile_job, nullptr, total, buf_floats, err);                              \
     }                                                                                               \
-    __global__ void __launch_bounds__(MP_RO_NT)                                                     \
+    __global__ void __launch_bounds__(MP_RO_NT_FWD)                                                 \
         NAME##_single(const __grid_constant__ MPJob job, int buf_floats, int *err)                  \
     {                                                                                               \
-        ro_run<C>(nullptr, nullptr, &job, job.ntiles, buf_floats, err);                              \
+        ro_run_fwd<C>(nullptr, nullptr, &job, job.ntiles, buf_floats, err);                          \
     }
 
 MP_RO_KERNELS(mp_ro_c1, 1)
@@ -554,6 +618,9 @@ static const void *mp_ro_fn(int c, bool single)
 
 size_t mp_ro_smem(int buf_floats) { return 256 + 2 * (size_t)buf_floats * 4 + 128; }
 
+// Threads of a launch: the forward kernels (c = 1, 3, 4) add the producer warp.
+static int mp_ro_block(int c) { return c < 8 ? MP_RO_NT_FWD : MP_RO_NT; }
+
 MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
 {
     static std::mutex mtx;
@@ -574,7 +641,7 @@ MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
         e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (e != cudaSuccess) return mp_cuda_status(e);
         // the opt-in maximum covers static and dynamic shared memory together
-        cudaFuncAttributes fa;
+        cudaFuncAttributes fa;   // (static shared memory of the kernel)
         e = cudaFuncGetAttributes(&fa, fn);
         if (e != cudaSuccess) return mp_cuda_status(e);
         e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
@@ -583,7 +650,7 @@ MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
     }
     if (ctas_per_sm) {
         int n = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mp_ro_fn(c, false), MP_RO_NT, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mp_ro_fn(c, false), mp_ro_block(c), smem);
         if (e != cudaSuccess) return mp_cuda_status(e);
         if (n < 1) return MP_ERROR_TOO_LARGE;
         *ctas_per_sm = n;
@@ -600,7 +667,7 @@ MPStatus mp_ro_launch(int c, const MPJob *jobs_dev, const int *tile_job, int tot
     if (grid > total) grid = total;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&jobs_dev, (void *)&tile_job, (void *)&total, (void *)&buf_floats, (void *)&err};
-    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_RO_NT), args, mp_ro_smem(buf_floats), s));
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(mp_ro_block(c)), args, mp_ro_smem(buf_floats), s));
 }
 
 MPStatus mp_ro_launch_single(int c, const MPJob &job, int buf_floats, int grid, int *err, cudaStream_t s)
@@ -611,5 +678,5 @@ MPStatus mp_ro_launch_single(int c, const MPJob &job, int buf_floats, int grid, 
     if (grid > job.ntiles) grid = job.ntiles;
     if (grid < 1) grid = 1;
     void *args[] = {(void *)&job, (void *)&buf_floats, (void *)&err};
-    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(MP_RO_NT), args, mp_ro_smem(buf_floats), s));
+    return mp_cuda_status(cudaLaunchKernel(fn, dim3(grid), dim3(mp_ro_block(c)), args, mp_ro_smem(buf_floats), s));
 }
