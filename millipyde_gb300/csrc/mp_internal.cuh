@@ -47,7 +47,7 @@ enum MPKind {
 __host__ __device__ constexpr int mp_ro_tw(int c) { return c == 1 ? 64 : 32; }
 __host__ __device__ constexpr int mp_ro_th(int c) { return c == 1 ? 64 : 32; }
 #define MP_RO_NT 256
-#define MP_RO_NT_FWD (MP_RO_NT + 32)   // forward rotate: sampling threads + a producer warp
+#define MP_RO_NT_WS (MP_RO_NT + 32)    // rotate and its dx: sampling threads + a producer warp
 
 // ---------------------------------------------------------------------------
 // Streaming gaussian geometry (host and device agree on it).  Rows are

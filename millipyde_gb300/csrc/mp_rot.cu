@@ -407,7 +407,7 @@ __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
     return smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
 }
 
-// Forward rotate, warp-specialised: MP_RO_NT sampling threads and one
+// Forward rotate and the adjoint's dx, warp-specialised: MP_RO_NT sampling threads and one
 // producer warp whose lane 0 copies each tile's job fields into its record
 // and issues its footprint's TMA.  Buffer k & 1 holds tile k; `full` says
 // its copy landed, `empty` that every sampling thread is done with it (each
@@ -415,10 +415,11 @@ __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
 // No block-wide barrier: sampling warps never wait for the issuing
 // thread's job-table reads or for each other.  Every wait is bounded; after
 // a timeout the producer lets its copies in flight land before it returns.
-template <int C>
-__device__ __forceinline__ void ro_run_fwd(const MPJob *jobs, const int *tile_job, const MPJob *one, int total,
-                                           int buf_floats, int *err)
+template <int C, int MODE = RO_FWD>
+__device__ __forceinline__ void ro_run_ws(const MPJob *jobs, const int *tile_job, const MPJob *one, int total,
+                                          int buf_floats, int *err)
 {
+    static_assert(MODE != RO_DTH, "the d theta mode reduces across the block: ro_run");
     extern __shared__ unsigned char mp_ro_smem[];
     unsigned char *base = ro_base(mp_ro_smem);
     uint64_t *full = reinterpret_cast<uint64_t *>(base);          // [2]
@@ -447,7 +448,7 @@ __device__ __forceinline__ void ro_run_fwd(const MPJob *jobs, const int *tile_jo
             const int ji = one ? 0 : __ldg(tile_job + t);
             const MPJob &J = one ? *one : jobs[ji];
             if (!one) mp_tensormap_acquire(&J.tmap);
-            ro_issue<C, RO_FWD>(J, ji, one ? t : t - J.tile0, bufs + b * buf_floats, full + b, recs + b);
+            ro_issue<C, MODE>(J, ji, one ? t : t - J.tile0, bufs + b * buf_floats, full + b, recs + b);
         }
         if (!ok) {
             atomicExch(err, MP_KERR_TIMEOUT);
@@ -466,7 +467,8 @@ __device__ __forceinline__ void ro_run_fwd(const MPJob *jobs, const int *tile_jo
         }
         const RoTile rec = recs[b];
         const MPJob &J = one ? *one : jobs[rec.jidx];
-        ro_tile<C>(J, rec, bufs + b * buf_floats);
+        if (MODE == RO_FWD) ro_tile<C>(J, rec, bufs + b * buf_floats);
+        else ro_adj_tile<C>(J, rec, bufs + b * buf_floats);
         mp_mbar_arrive(empty + b);
     }
 }
@@ -563,23 +565,24 @@ __device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, c
 }  // namespace
 
 #define MP_RO_KERNELS(NAME, C)                                                                       \
-    __global__ void __launch_bounds__(MP_RO_NT_FWD) NAME##_batch(const MPJob *__restrict__ jobs,    \
+    __global__ void __launch_bounds__(MP_RO_NT_WS) NAME##_batch(const MPJob *__restrict__ jobs,    \
                                                                  const int *__restrict__ tile_job,  \
                                                                  int total, int buf_floats, int *err) \
     {                                                                                               \
-        ro_run_fwd<C>(jobs, tile_job, nullptr, total, buf_floats, err);                              \
+        ro_run_ws<C>(jobs, tile_job, nullptr, total, buf_floats, err);                              \
     }                                                                                               \
-    __global__ void __launch_bounds__(MP_RO_NT_FWD)                                                 \
+    __global__ void __launch_bounds__(MP_RO_NT_WS)                                                 \
         NAME##_single(const __grid_constant__ MPJob job, int buf_floats, int *err)                  \
     {                                                                                               \
-        ro_run_fwd<C>(nullptr, nullptr, &job, job.ntiles, buf_floats, err);                          \
+        ro_run_ws<C>(nullptr, nullptr, &job, job.ntiles, buf_floats, err);                          \
     }
 
 MP_RO_KERNELS(mp_ro_c1, 1)
 MP_RO_KERNELS(mp_ro_c3, 3)
 MP_RO_KERNELS(mp_ro_c4, 4)
 
-// The adjoint's modes (batch launches only).
+// The adjoint's modes (batch launches only): dx warp-specialised, d theta
+// with block-wide barriers (it reduces across the block).
 #define MP_RO_MODE_KERNEL(NAME, C, MODE)                                                             \
     __global__ void __launch_bounds__(MP_RO_NT) NAME(const MPJob *__restrict__ jobs,                 \
                                                      const int *__restrict__ tile_job, int total,    \
@@ -587,10 +590,17 @@ MP_RO_KERNELS(mp_ro_c4, 4)
     {                                                                                               \
         ro_run<C, MODE>(jobs, tile_job, nullptr, total, buf_floats, err);                            \
     }
+#define MP_RO_ADJ_KERNEL(NAME, C)                                                                    \
+    __global__ void __launch_bounds__(MP_RO_NT_WS) NAME(const MPJob *__restrict__ jobs,              \
+                                                        const int *__restrict__ tile_job, int total, \
+                                                        int buf_floats, int *err)                    \
+    {                                                                                               \
+        ro_run_ws<C, RO_ADJ>(jobs, tile_job, nullptr, total, buf_floats, err);                       \
+    }
 
-MP_RO_MODE_KERNEL(mp_ro_adj_c1, 1, RO_ADJ)
-MP_RO_MODE_KERNEL(mp_ro_adj_c3, 3, RO_ADJ)
-MP_RO_MODE_KERNEL(mp_ro_adj_c4, 4, RO_ADJ)
+MP_RO_ADJ_KERNEL(mp_ro_adj_c1, 1)
+MP_RO_ADJ_KERNEL(mp_ro_adj_c3, 3)
+MP_RO_ADJ_KERNEL(mp_ro_adj_c4, 4)
 MP_RO_MODE_KERNEL(mp_ro_dth_c1, 1, RO_DTH)
 MP_RO_MODE_KERNEL(mp_ro_dth_c3, 3, RO_DTH)
 MP_RO_MODE_KERNEL(mp_ro_dth_c4, 4, RO_DTH)
@@ -618,8 +628,8 @@ static const void *mp_ro_fn(int c, bool single)
 
 size_t mp_ro_smem(int buf_floats) { return 256 + 2 * (size_t)buf_floats * 4 + 128; }
 
-// Threads of a launch: the forward kernels (c = 1, 3, 4) add the producer warp.
-static int mp_ro_block(int c) { return c < 8 ? MP_RO_NT_FWD : MP_RO_NT; }
+// Threads of a launch: the forward and dx kernels add the producer warp.
+static int mp_ro_block(int c) { return c < 8 * RO_DTH ? MP_RO_NT_WS : MP_RO_NT; }
 
 MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
 {
