@@ -119,21 +119,31 @@ __device__ __forceinline__ void mp_pw_back(const PwOp &o, const float v[4], int 
     }
 }
 
-// One 256 x 4 tile of a pointwise run.  The ops are walked by loops that
-// are not unrolled (one copy of each op's code): for op k from last to
-// first, its input is recomputed from x through ops 0..k-1 (runs are short),
-// then g is pulled back through op k.
+// One 256 x 4 tile of a pointwise run of NS ops (NS = 0: the run's length
+// is read from the job).  For op k from last to first, its input is
+// recomputed from x through ops 0..k-1 (runs are short), then g is pulled
+// back through op k.  Runs of 1 to 3 ops (nearly all) are compiled with the
+// op loops unrolled and one accumulator set per op; longer runs walk the ops
+// with loops that are not unrolled.
+template <int NS>
 __device__ void mp_point_adj_tile(const MPJob &J, int t, float *red)
 {
+    constexpr int NP = NS ? NS : MP_MAX_PW;   // accumulator sets
     const int ty = t / J.tiles_x, tx = t - ty * J.tiles_x;
     const int x = tx * 256 + threadIdx.x;
-    const int n = J.pro.n, cin = J.cin;
+    const int n = NS ? NS : J.pro.n, cin = J.cin;
+    PwOp ops[NS ? NS : 1];
+    if constexpr (NS > 0) {
+#pragma unroll
+        for (int k = 0; k < NS; ++k) ops[k] = J.pro.op[k];
+    }
+    auto op_at = [&](int k) -> PwOp { if constexpr (NS > 0) return ops[k]; else return J.pro.op[k]; };
     int cout = cin;
     for (int k = 0; k < n; ++k)
-        if (J.pro.op[k].op == MP_OP_RGB2GREY && cout >= 3) cout = 1;
-    float pacc[MP_MAX_PW][3];
+        if (op_at(k).op == MP_OP_RGB2GREY && cout >= 3) cout = 1;
+    float pacc[NP][3];
 #pragma unroll
-    for (int k = 0; k < MP_MAX_PW; ++k) pacc[k][0] = pacc[k][1] = pacc[k][2] = 0.f;
+    for (int k = 0; k < NP; ++k) pacc[k][0] = pacc[k][1] = pacc[k][2] = 0.f;
     if (x < J.w) {
         // the tile's 4 rows are loaded before any is processed (their loads
         // overlap instead of waiting on each row's compute)
@@ -154,26 +164,43 @@ __device__ void mp_point_adj_tile(const MPJob &J, int t, float *red)
             const int y = ty * 4 + i;
             if (y >= J.h) break;
             float g[4] = {g0[i][0], g0[i][1], g0[i][2], g0[i][3]};
-#pragma unroll 1
-            for (int k = n - 1; k >= 0; --k) {
-                float v[4] = {x0[i][0], x0[i][1], x0[i][2], x0[i][3]};
-                int c = cin;
-#pragma unroll 1
-                for (int j = 0; j < k; ++j) {
-                    const PwOp o = J.pro.op[j];
-                    c = mp_pw_op(o.op, o.p0, o.p1, o.p2, v, c);
+            if constexpr (NS > 0) {
+#pragma unroll
+                for (int k = NS - 1; k >= 0; --k) {
+                    float v[4] = {x0[i][0], x0[i][1], x0[i][2], x0[i][3]};
+                    int c = cin;
+#pragma unroll
+                    for (int j = 0; j < k; ++j) c = mp_pw_op(ops[j].op, ops[j].p0, ops[j].p1, ops[j].p2, v, c);
+                    float gi[4], pa[3] = {0.f, 0.f, 0.f};
+                    mp_pw_back(ops[k], v, c, g, gi, pa);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) g[q] = gi[q];
+                    pacc[k][0] += pa[0];
+                    pacc[k][1] += pa[1];
+                    pacc[k][2] += pa[2];
                 }
-                float gi[4], pa[3] = {0.f, 0.f, 0.f};
-                mp_pw_back(J.pro.op[k], v, c, g, gi, pa);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) g[q] = gi[q];
-#pragma unroll
-                for (int kk = 0; kk < MP_MAX_PW; ++kk)
-                    if (kk == k) {
-                        pacc[kk][0] += pa[0];
-                        pacc[kk][1] += pa[1];
-                        pacc[kk][2] += pa[2];
+            } else {
+#pragma unroll 1
+                for (int k = n - 1; k >= 0; --k) {
+                    float v[4] = {x0[i][0], x0[i][1], x0[i][2], x0[i][3]};
+                    int c = cin;
+#pragma unroll 1
+                    for (int j = 0; j < k; ++j) {
+                        const PwOp o = J.pro.op[j];
+                        c = mp_pw_op(o.op, o.p0, o.p1, o.p2, v, c);
                     }
+                    float gi[4], pa[3] = {0.f, 0.f, 0.f};
+                    mp_pw_back(J.pro.op[k], v, c, g, gi, pa);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) g[q] = gi[q];
+#pragma unroll
+                    for (int kk = 0; kk < MP_MAX_PW; ++kk)
+                        if (kk == k) {
+                            pacc[kk][0] += pa[0];
+                            pacc[kk][1] += pa[1];
+                            pacc[kk][2] += pa[2];
+                        }
+                }
             }
             float *d = J.dst + (size_t)y * J.dst_pitch + (size_t)x * cin;
 #pragma unroll
@@ -183,13 +210,14 @@ __device__ void mp_point_adj_tile(const MPJob &J, int t, float *red)
     }
     if (!J.acc) return;
     for (int k = 0; k < n; ++k) {
-        const int np = (J.pro.op[k].op == MP_OP_BRIGHTNESS || J.pro.op[k].op == MP_OP_BRIGHTNESS_OUT) ? 1
-                     : (J.pro.op[k].op == MP_OP_ADJUST_GAMMA) ? 2
-                     : (J.pro.op[k].op == MP_OP_COLORIZE) ? 3 : 0;
+        const int op = op_at(k).op;
+        const int np = (op == MP_OP_BRIGHTNESS || op == MP_OP_BRIGHTNESS_OUT) ? 1
+                     : (op == MP_OP_ADJUST_GAMMA) ? 2
+                     : (op == MP_OP_COLORIZE) ? 3 : 0;
         for (int j = 0; j < np; ++j) {
             float val = 0.f;
 #pragma unroll
-            for (int kk = 0; kk < MP_MAX_PW; ++kk)
+            for (int kk = 0; kk < NP; ++kk)
 #pragma unroll
                 for (int jj = 0; jj < 3; ++jj)
                     if (kk == k && jj == j) val = pacc[kk][jj];
@@ -304,7 +332,12 @@ __global__ void __launch_bounds__(MP_THREADS) mp_point_adjoint_batch(const MPJob
     __shared__ float red[32];
     const int t = blockIdx.x;
     const MPJob &J = jobs[__ldg(tile_job + t)];
-    mp_point_adj_tile(J, t - J.tile0, red);
+    switch (J.pro.n) {
+    case 1: mp_point_adj_tile<1>(J, t - J.tile0, red); break;
+    case 2: mp_point_adj_tile<2>(J, t - J.tile0, red); break;
+    case 3: mp_point_adj_tile<3>(J, t - J.tile0, red); break;
+    default: mp_point_adj_tile<0>(J, t - J.tile0, red); break;
+    }
 }
 
 __global__ void __launch_bounds__(MP_THREADS) mp_rotate_adjoint_batch(const MPJob *__restrict__ jobs,
