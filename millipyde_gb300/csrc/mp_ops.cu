@@ -1870,6 +1870,7 @@ extern "C" MPStatus mpk_pipeline_produce(const MPStage *stages, int nstages, MPO
 // Host-buffer batch with copy/compute overlap.
 // ---------------------------------------------------------------------------
 #define MP_HOST_CHUNK_BYTES (192ull << 20)
+#define MP_HOST_SLOTS 3
 
 static cudaStream_t mp_copy_stream(int dev, int which)
 {
@@ -1934,19 +1935,22 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
         max_in = std::max(max_in, cin);
         max_out = std::max(max_out, cout);
     }
-    const int nslots = chunks.size() > 1 ? 2 : 1;
-    void *ibuf[2] = {nullptr, nullptr}, *obuf[2] = {nullptr, nullptr};
+    // three slots: the copy of chunk k + 3 waits for chunk k's compute, and
+    // chunk k's compute for chunk k - 3's results to leave, so the two link
+    // directions and the kernels run with a chunk of slack between them
+    const int nslots = (int)std::min<size_t>(MP_HOST_SLOTS, chunks.size());
+    void *ibuf[MP_HOST_SLOTS] = {}, *obuf[MP_HOST_SLOTS] = {};
     // Packed landing buffers: an image whose host rows are packed crosses
     // the link as one 1-D copy and is re-pitched on the device (and the
     // reverse for results).  Measured on GB300: 2-D host-to-device copies
     // of 1.5 KB rows ran at 35 GB/s (21 GB/s per 129-row image), of 6.9 KB
     // rows at 107 GB/s, a 1-D copy at 212 GB/s.
-    void *lin[2] = {nullptr, nullptr}, *lout[2] = {nullptr, nullptr};
+    void *lin[MP_HOST_SLOTS] = {}, *lout[MP_HOST_SLOTS] = {};
     std::vector<MPPlan *> plans(chunks.size(), nullptr);
-    cudaEvent_t ev[4][2];
+    cudaEvent_t ev[4][MP_HOST_SLOTS] = {};
     bool ev_ok = true;
     for (int a = 0; a < 4; ++a)
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < MP_HOST_SLOTS; ++b)
             ev_ok &= cudaEventCreateWithFlags(&ev[a][b], cudaEventDisableTiming) == cudaSuccess;
     enum { E_H2D = 0, E_COMP = 1, E_D2H = 2, E_ALLOC = 3 };
     MPStatus st = ev_ok ? MILLIPYDE_SUCCESS : MP_ERROR_CUDA;
@@ -2047,14 +2051,15 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     for (MPPlan *p : plans) mpk_plan_destroy(p);
     for (MPPlan *p : rin) mpk_plan_destroy(p);
     for (MPPlan *p : rout) mpk_plan_destroy(p);
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < MP_HOST_SLOTS; ++s) {
         mp_free_async(lin[s], cs);
         mp_free_async(lout[s], cs);
         mp_free_async(ibuf[s], cs);
         mp_free_async(obuf[s], cs);
     }
     for (int a = 0; a < 4; ++a)
-        for (int b = 0; b < 2; ++b) cudaEventDestroy(ev[a][b]);
+        for (int b = 0; b < MP_HOST_SLOTS; ++b)
+            if (ev[a][b]) cudaEventDestroy(ev[a][b]);
     if (st != MILLIPYDE_SUCCESS) return st;
     return mp_check_device_error(cs);
 }
