@@ -1938,6 +1938,9 @@ extern "C" MPStatus mpk_pipeline_run_host(const MPStage *stages, int nstages, co
     // three slots: the copy of chunk k + 3 waits for chunk k's compute, and
     // chunk k's compute for chunk k - 3's results to leave, so the two link
     // directions and the kernels run with a chunk of slack between them
+    // (measured on 1000 ragged images, 8.08 GB over the link: 36.0 ms against
+    // 36.2 with two slots; the same copies with no kernels take 34.4 ms, so
+    // the link bounds the call)
     const int nslots = (int)std::min<size_t>(MP_HOST_SLOTS, chunks.size());
     void *ibuf[MP_HOST_SLOTS] = {}, *obuf[MP_HOST_SLOTS] = {};
     // Packed landing buffers: an image whose host rows are packed crosses
