@@ -358,6 +358,15 @@ __device__ __forceinline__ void mp_mbar_arrive(uint64_t *bar)
     asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mp_smem_addr(bar)) : "memory");
 }
 
+// Arrive once `dep` is computed: a thread whose loaded values end in a
+// register sum (no store) makes its arrive depend on the sum, so the loads
+// have completed before the buffer can be refilled.
+__device__ __forceinline__ void mp_mbar_arrive_after(uint64_t *bar, float dep)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mp_smem_addr(bar)), "f"(dep)
+                 : "memory");
+}
+
 __device__ __forceinline__ bool mp_mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;

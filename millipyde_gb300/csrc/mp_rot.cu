@@ -407,19 +407,22 @@ __device__ __forceinline__ unsigned char *ro_base(unsigned char *smem_raw)
     return smem_raw + ((128 - (int)(mp_smem_addr(smem_raw) & 127)) & 127);
 }
 
-// Forward rotate and the adjoint's dx, warp-specialised: MP_RO_NT sampling threads and one
-// producer warp whose lane 0 copies each tile's job fields into its record
-// and issues its footprint's TMA.  Buffer k & 1 holds tile k; `full` says
-// its copy landed, `empty` that every sampling thread is done with it (each
-// arrives after its tile's stores, which consume every value it loaded).
+// Persistent loop over tiles t = first, first + step, ... of a tile -> job
+// map (or of one job when `jobs` is null), warp-specialised: MP_RO_NT
+// sampling threads and one producer warp whose lane 0 copies each tile's
+// job fields into its record and issues its footprint's TMA.  Buffer k & 1
+// holds tile k; `full` says its copy landed, `empty` that every sampling
+// thread is done with it (each arrives after its tile's stores, or in the
+// d theta mode after its running sum, which consume every value it loaded).
 // No block-wide barrier: sampling warps never wait for the issuing
-// thread's job-table reads or for each other.  Every wait is bounded; after
-// a timeout the producer lets its copies in flight land before it returns.
+// thread's job-table reads or for each other; the d theta mode reduces its
+// sums per warp (one FP64 atomic per warp when the CTA moves to another
+// image).  Every wait is bounded; after a timeout the producer lets its
+// copies in flight land before it returns.
 template <int C, int MODE = RO_FWD>
 __device__ __forceinline__ void ro_run_ws(const MPJob *jobs, const int *tile_job, const MPJob *one, int total,
                                           int buf_floats, int *err)
 {
-    static_assert(MODE != RO_DTH, "the d theta mode reduces across the block: ro_run");
     extern __shared__ unsigned char mp_ro_smem[];
     unsigned char *base = ro_base(mp_ro_smem);
     uint64_t *full = reinterpret_cast<uint64_t *>(base);          // [2]
@@ -458,105 +461,39 @@ __device__ __forceinline__ void ro_run_ws(const MPJob *jobs, const int *tile_job
         }
         return;
     }
+    // RO_DTH: this thread's running d theta share for job `cur`
+    const MPJob *cur = nullptr;
+    float dth = 0.f;
+    auto flush = [&]() {
+        float v = dth;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(cur->acc, (double)v);
+        dth = 0.f;
+    };
     int k = 0;
     for (int t = first; t < total; t += step, ++k) {
         const int b = k & 1;
-        if (!mp_mbar_wait_bounded(full + b, (uint32_t)(k >> 1) & 1u)) {
+        // the warp leaves together (the d theta mode shuffles across it)
+        if (!__all_sync(0xffffffffu, mp_mbar_wait_bounded(full + b, (uint32_t)(k >> 1) & 1u))) {
             atomicExch(err, MP_KERR_TIMEOUT);
             return;
         }
         const RoTile rec = recs[b];
         const MPJob &J = one ? *one : jobs[rec.jidx];
-        if (MODE == RO_FWD) ro_tile<C>(J, rec, bufs + b * buf_floats);
-        else ro_adj_tile<C>(J, rec, bufs + b * buf_floats);
-        mp_mbar_arrive(empty + b);
-    }
-}
-
-// Persistent loop over tiles t = first, first + step, ... of a tile -> job map
-// (or of one job when `jobs` is null).  Buffer k & 1 holds tile k's footprint.
-template <int C, int MODE = RO_FWD>
-__device__ __forceinline__ void ro_run(const MPJob *jobs, const int *tile_job, const MPJob *one, int total,
-                                       int buf_floats, int *err)
-{
-    __shared__ float red[MP_RO_NT / 32];
-    // RO_DTH: this thread's running d theta share for job `cur`; flushed
-    // (block sum, one FP64 atomic) when the CTA moves to another job
-    const MPJob *cur = nullptr;
-    float dth = 0.f;
-    auto flush = [&]() {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) dth += __shfl_down_sync(0xffffffffu, dth, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dth;
-        __syncthreads();
-        if (threadIdx.x == 0 && cur) {
-            float tot = 0.f;
-            for (int w = 0; w < MP_RO_NT / 32; ++w) tot += red[w];
-            atomicAdd(cur->acc, (double)tot);
-        }
-        __syncthreads();
-        dth = 0.f;
-    };
-    extern __shared__ unsigned char mp_ro_smem[];
-    unsigned char *base = ro_base(mp_ro_smem);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(base);
-    RoTile *recs = reinterpret_cast<RoTile *>(base + 16);   // one record per buffer
-    float *bufs = reinterpret_cast<float *>(base + 256);
-    if (threadIdx.x == 0) {
-        mp_mbar_init(bars, 1);
-        mp_mbar_init(bars + 1, 1);
-        mp_fence_barrier_init();
-    }
-    __syncthreads();
-    const int first = blockIdx.x, step = gridDim.x;
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < 2; ++k) {
-            const int t = first + k * step;
-            if (t >= total) break;
-            const int ji = one ? 0 : __ldg(tile_job + t);
-            const MPJob &J = one ? *one : jobs[ji];
-            if (!one) mp_tensormap_acquire(&J.tmap);
-            ro_issue<C, MODE>(J, ji, one ? t : t - J.tile0, bufs + k * buf_floats, bars + k, recs + k);
-        }
-    }
-    int k = 0;
-    for (int t = first; t < total; t += step, ++k) {
-        const float *buf = bufs + (k & 1) * buf_floats;
-        const bool ok = mp_mbar_wait_bounded(bars + (k & 1), (uint32_t)(k >> 1) & 1u);
-        if (!__syncthreads_and(ok)) {
-            if (threadIdx.x == 0) atomicExch(err, MP_KERR_TIMEOUT);
-            // drain the other buffer's copy if one was issued
-            if (t + step < total) mp_mbar_wait_bounded(bars + ((k + 1) & 1), (uint32_t)((k + 1) >> 1) & 1u);
-            return;
-        }
-        const RoTile rec = recs[k & 1];
-        const MPJob &J = one ? *one : jobs[rec.jidx];
         if (MODE == RO_FWD) {
-            ro_tile<C>(J, rec, buf);
+            ro_tile<C>(J, rec, bufs + b * buf_floats);
+            mp_mbar_arrive(empty + b);
         } else if (MODE == RO_ADJ) {
-            ro_adj_tile<C>(J, rec, buf);
+            ro_adj_tile<C>(J, rec, bufs + b * buf_floats);
+            mp_mbar_arrive(empty + b);
         } else {
             if (cur != &J) {
                 if (cur) flush();
                 cur = &J;
             }
-            dth += ro_dth_tile<C>(J, rec, buf);
-        }
-        // buffer and record k & 1 are free again.  The d theta sum lives in a
-        // register: the barrier's predicate depends on it, so this tile's
-        // shared-memory loads have completed before the buffer is refilled by
-        // TMA (the forward and dx modes store their results first).
-        if (MODE == RO_DTH) __syncthreads_or(dth == 3.0e38f);
-        else __syncthreads();
-        if (threadIdx.x == 0) {
-            const int tn = t + 2 * step;
-            if (tn < total) {
-                const int jn = one ? 0 : __ldg(tile_job + tn);
-                const MPJob &Jn = one ? *one : jobs[jn];
-                if (!one) mp_tensormap_acquire(&Jn.tmap);
-                ro_issue<C, MODE>(Jn, jn, one ? tn : tn - Jn.tile0, bufs + (k & 1) * buf_floats, bars + (k & 1),
-                                  recs + (k & 1));
-            }
+            dth += ro_dth_tile<C>(J, rec, bufs + b * buf_floats);
+            mp_mbar_arrive_after(empty + b, dth);
         }
     }
     if (MODE == RO_DTH && cur) flush();
@@ -581,26 +518,18 @@ MP_RO_KERNELS(mp_ro_c1, 1)
 MP_RO_KERNELS(mp_ro_c3, 3)
 MP_RO_KERNELS(mp_ro_c4, 4)
 
-// The adjoint's modes (batch launches only): dx warp-specialised, d theta
-// with block-wide barriers (it reduces across the block).
+// The adjoint's modes (batch launches only).
 #define MP_RO_MODE_KERNEL(NAME, C, MODE)                                                             \
-    __global__ void __launch_bounds__(MP_RO_NT) NAME(const MPJob *__restrict__ jobs,                 \
-                                                     const int *__restrict__ tile_job, int total,    \
-                                                     int buf_floats, int *err)                       \
-    {                                                                                               \
-        ro_run<C, MODE>(jobs, tile_job, nullptr, total, buf_floats, err);                            \
-    }
-#define MP_RO_ADJ_KERNEL(NAME, C)                                                                    \
     __global__ void __launch_bounds__(MP_RO_NT_WS) NAME(const MPJob *__restrict__ jobs,              \
                                                         const int *__restrict__ tile_job, int total, \
                                                         int buf_floats, int *err)                    \
     {                                                                                               \
-        ro_run_ws<C, RO_ADJ>(jobs, tile_job, nullptr, total, buf_floats, err);                       \
+        ro_run_ws<C, MODE>(jobs, tile_job, nullptr, total, buf_floats, err);                         \
     }
 
-MP_RO_ADJ_KERNEL(mp_ro_adj_c1, 1)
-MP_RO_ADJ_KERNEL(mp_ro_adj_c3, 3)
-MP_RO_ADJ_KERNEL(mp_ro_adj_c4, 4)
+MP_RO_MODE_KERNEL(mp_ro_adj_c1, 1, RO_ADJ)
+MP_RO_MODE_KERNEL(mp_ro_adj_c3, 3, RO_ADJ)
+MP_RO_MODE_KERNEL(mp_ro_adj_c4, 4, RO_ADJ)
 MP_RO_MODE_KERNEL(mp_ro_dth_c1, 1, RO_DTH)
 MP_RO_MODE_KERNEL(mp_ro_dth_c3, 3, RO_DTH)
 MP_RO_MODE_KERNEL(mp_ro_dth_c4, 4, RO_DTH)
@@ -628,8 +557,8 @@ static const void *mp_ro_fn(int c, bool single)
 
 size_t mp_ro_smem(int buf_floats) { return 256 + 2 * (size_t)buf_floats * 4 + 128; }
 
-// Threads of a launch: the forward and dx kernels add the producer warp.
-static int mp_ro_block(int c) { return c < 8 * RO_DTH ? MP_RO_NT_WS : MP_RO_NT; }
+// Threads of a launch: the sampling threads plus the producer warp.
+static int mp_ro_block(int) { return MP_RO_NT_WS; }
 
 MPStatus mp_ro_prepare(int c, size_t smem, int *ctas_per_sm)
 {
