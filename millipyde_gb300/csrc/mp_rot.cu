@@ -311,17 +311,24 @@ __device__ __forceinline__ void ro_adj_tile(const MPJob &J, const RoTile &T, con
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
         long long sxr, syr;
         ro_src_fixed(J, px0, py0, sxr, syr);
+        // candidates in 8.24 fixed point relative to q: each row starts from
+        // its exact position, the 4 candidates of a row step by the rounded
+        // 8.24 step (drift below 3 * 2^-24 pixel)
+        const long long qxf = (long long)qx << MP_FIX_FRAC, qyf = (long long)qy << MP_FIX_FRAC;
+        const int c2s = (int)(c2 >> (MP_FIX_FRAC - 24)), s2s = (int)(s2 >> (MP_FIX_FRAC - 24));
 #pragma unroll
         for (int jy = 0; jy < 4; ++jy) {
             const int py = py0 + jy;
             const bool yok = py >= 0 && py < H;
-            long long sx = sxr, sy = syr;
+            int lx = (int)((sxr - qxf) >> (MP_FIX_FRAC - 24)), ly = (int)((syr - qyf) >> (MP_FIX_FRAC - 24));
 #pragma unroll
             for (int jx = 0; jx < 4; ++jx) {
                 const int px = px0 + jx;
-                const int ex = qx - (int)(sx >> MP_FIX_FRAC), ey = qy - (int)(sy >> MP_FIX_FRAC);
+                // floor(s) - q is -1 or 0 when q is one of the sample's neighbours
+                const int ex = -(lx >> 24), ey = -(ly >> 24);
                 if (yok && px >= 0 && px < W && (unsigned)ex <= 1u && (unsigned)ey <= 1u) {
-                    const float fx = ro_frac24(sx), fy = ro_frac24(sy);
+                    const float fx = (float)(lx & 0xFFFFFF) * 5.9604644775390625e-8f;
+                    const float fy = (float)(ly & 0xFFFFFF) * 5.9604644775390625e-8f;
                     const float w = (ey ? fy : 1.0f - fy) * (ex ? fx : 1.0f - fx);
                     const int ox = px - bx, oy = py - by;
                     if ((unsigned)ox < (unsigned)bpx && (unsigned)oy < (unsigned)bh) {
@@ -334,8 +341,8 @@ __device__ __forceinline__ void ro_adj_tile(const MPJob &J, const RoTile &T, con
                         for (int c = 0; c < C; ++c) acc[c] = fmaf(w, __ldg(v + c), acc[c]);
                     }
                 }
-                sx += c2;
-                sy += s2;
+                lx += c2s;
+                ly += s2s;
             }
             sxr -= s2;
             syr += c2;
@@ -520,7 +527,7 @@ MP_RO_KERNELS(mp_ro_c4, 4)
 
 // The adjoint's modes (batch launches only).
 #define MP_RO_MODE_KERNEL(NAME, C, MODE)                                                             \
-    __global__ void __launch_bounds__(MP_RO_NT_WS) NAME(const MPJob *__restrict__ jobs,              \
+    __global__ void __launch_bounds__(MP_RO_NT_WS, 4) NAME(const MPJob *__restrict__ jobs,           \
                                                         const int *__restrict__ tile_job, int total, \
                                                         int buf_floats, int *err)                    \
     {                                                                                               \
