@@ -166,6 +166,7 @@ static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
     cur.hin = cur.hout = h;
     cur.win = cur.wout = w;
     int c = cin;
+    int core_idx = -1;   // index of the current segment's core op
     for (size_t oi = 0; oi < ops.size(); ++oi) {
         const ROp &r = ops[oi];
         if (mp_is_pointwise(r.op)) {
@@ -177,13 +178,16 @@ static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
             // preserving streaming blur cannot reduce channels on its store,
             // and the tile kernel that can was slower than the streaming blur
             // plus a pointwise pass (64 x 512x512 RGB, sigma 1..3: 402 us
-            // against about 200 + 60 us).
+            // against about 200 + 60 us).  Without a flip in the gaussian's
+            // segment its whole epilogue moves along: the pointwise pass costs
+            // the same, and the segment boundary is then the blur's own
+            // output, the intermediate a differentiable chain's backward
+            // needs (saved by the forward instead of recomputed).
             if (r.op == MP_OP_RGB2GREY && cur.core_op == MP_OP_GAUSSIAN) {
                 bool spatial_after = false;
                 for (size_t q = oi + 1; q < ops.size(); ++q)
                     spatial_after = spatial_after || !(mp_is_pointwise(ops[q].op) || ops[q].op == MP_OP_FLIPLR);
                 if (!spatial_after) {
-                    segs.push_back(cur);
                     Seg nx;
                     memset(&nx, 0, sizeof(nx));
                     nx.kind = MPK_POINT;
@@ -192,6 +196,12 @@ static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
                     nx.hin = nx.hout = cur.hout;
                     nx.win = nx.wout = cur.wout;
                     nx.op0 = (int)oi;
+                    if (!cur.flip && cur.epi.n > 0 && cur.epi.n < MP_MAX_PW) {
+                        nx.pro = cur.epi;              // channel-preserving ops: c is unchanged
+                        nx.op0 = core_idx + 1;
+                        memset(&cur.epi, 0, sizeof(cur.epi));
+                    }
+                    segs.push_back(cur);
                     cur = nx;
                 }
             }
@@ -233,6 +243,7 @@ static MPStatus mp_segment(const std::vector<ROp> &ops, int cin, int h, int w,
             cur = nx;
         }
         cur.core_op = r.op;
+        core_idx = (int)oi;
         cur.core_p[0] = r.p[0];
         cur.core_p[1] = r.p[1];
         cur.core_p[2] = r.p[2];

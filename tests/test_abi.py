@@ -166,8 +166,11 @@ def test_chain_saved_layout():
         assert L.mpk_chain_saved_layout(ops, n, B, H, W, Cc, C.byref(cnt), idx, off, C.byref(nb)) == 0
         return [idx[i] for i in range(cnt.value)], [off[i] for i in range(cnt.value)], nb.value
 
-    # rgb2grey after a colour gaussian opens a pointwise segment of its own
-    assert layout(["rotate", "gaussian", "adjust_gamma", "rgb2grey"]) == ([1, 3], [0, 480], 2 * 480)
+    # rgb2grey after a colour gaussian opens a pointwise segment of its own,
+    # taking the gaussian's epilogue along (the boundary is the blur's output)
+    assert layout(["rotate", "gaussian", "adjust_gamma", "rgb2grey"]) == ([1, 2], [0, 480], 2 * 480)
+    # with a flip in the gaussian's segment only the grey moves
+    assert layout(["gaussian", "fliplr", "adjust_gamma", "rgb2grey"]) == ([3], [0], 480)
     assert layout(["gaussian", "rotate", "brightness"]) == ([1], [0], 2 * 5 * 4 * 3 * 4)
     # the grey prologue joins the gaussian; the intermediate has one channel
     assert layout(["rgb2grey", "gaussian", "rotate", "adjust_gamma"]) == ([2], [0], 2 * 5 * 4 * 1 * 4)
