@@ -46,18 +46,6 @@
 #ifndef MP_VH_PAIR_RMAX
 #define MP_VH_PAIR_RMAX 4
 #endif
-// Row pairing in the radius-bucket kernels (256 threads, 1 CTA per SM):
-// measured slower (8192x8192 RGB, radius 24: 97.7 against 87.5 ms for a
-// training step with two such blurs per image), so off.
-// Horizontal pass of the channel-preserving and bucket kernels with
-// adjacent outputs packed in f32x2 pairs where their operands are an
-// aligned register pair (1 = on).
-#ifndef MP_VH_HPACK
-#define MP_VH_HPACK 1
-#endif
-#ifndef MP_VH_PAIR_BIG
-#define MP_VH_PAIR_BIG 0
-#endif
 
 namespace mp_vh {
 
@@ -164,8 +152,11 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
     constexpr int NW2 = BIG ? R + 1 : NTAP;               // tap registers
     // the plain one-channel family computes two output rows per
     // horizontal work item as packed pairs, and so does the channel-
-    // preserving family up to radius MP_VH_PAIR_RMAX
-    constexpr bool PAIR = (BIG ? MP_VH_PAIR_BIG != 0 : (CM == 1 || R <= MP_VH_PAIR_RMAX)) && !DOT;
+    // preserving family up to radius MP_VH_PAIR_RMAX; the radius buckets do
+    // not (256 threads, 1 CTA per SM: paired measured slower, 97.7 against
+    // 87.5 ms for a training step with two radius-24 blurs per 8192x8192 RGB
+    // image)
+    constexpr bool PAIR = !BIG && !DOT && (CM == 1 || R <= MP_VH_PAIR_RMAX);
     constexpr int R8 = (R + 3) & ~3;                      // window row padding (2*R8 is a multiple of 8)
     constexpr int D = R8 - R;                             // tap offset inside the window
     constexpr int NWIN = VR + 2 * R8;
@@ -492,7 +483,7 @@ __device__ __noinline__ void vh_item(const MPJob &J, int lt, float *smem, uint32
                         }
                         o[k] = a0 + a1;
                     }
-                } else if constexpr (!DOT && MP_VH_HPACK) {
+                } else if constexpr (!DOT) {
                     // taps CM floats apart: consume the tile row in order so
                     // that only the 8 sums stay live.  Outputs 2j and 2j + 1
                     // use the same tap at positions p and p + 1: where p is
